@@ -437,6 +437,41 @@ KHS_API KhsResult khsxCopyContactRecords(const KhsSolver *solver,
                                          KhsxContactRecord *records,
                                          uint32_t capacity);
 
+/* Broad + narrow phase of every element at the caller's state q (6 values
+   per internal node, as khsxCopyState returns) against the collider as
+   the last substep left it.  Does not change the solver state; records as
+   in khsxCopyContactRecords.  This is the integer contact work of one
+   evaluation, exposed so it can be compared bit for bit. */
+KHS_API KhsResult khsxQueryContacts(KhsSolver *solver, const double *q,
+                                    uint64_t dof_count,
+                                    KhsxContactRecord *records,
+                                    uint32_t capacity);
+
+/* ---- measurement ------------------------------------------------------- */
+
+/* With profiling on, every kernel launch of the solver is bracketed by CUDA
+   events on the solver's stream and the device time is accumulated per
+   kernel.  Off by default. */
+KHS_API KhsResult khsxSetProfiling(KhsSolver *solver, uint32_t enable);
+
+typedef struct KhsxKernelTiming {
+    char name[40];
+    uint64_t launches;
+    double total_milliseconds;
+} KhsxKernelTiming;
+
+/* Writes up to capacity entries, returns the number of kernels timed since
+   profiling was enabled (or since the last reset). */
+KHS_API uint32_t khsxGetKernelTimings(const KhsSolver *solver, KhsxKernelTiming *timings, uint32_t capacity);
+KHS_API KhsResult khsxResetKernelTimings(KhsSolver *solver);
+
+/* Kernels launched by this solver since it was built. */
+KHS_API uint64_t khsxGetKernelLaunchCount(const KhsSolver *solver);
+
+/* Measures the FP64 and FP32 FMA-pipe throughput of device 0 with a
+   dependent-chain-free FMA kernel (TFLOP/s, 2 flops per FMA). */
+KHS_API KhsResult khsxMeasurePipePeaks(double *fp64_tflops, double *fp32_tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,434 @@
+// Per-element and per-contact FP64 math of the GB300 solver.
+//
+// Everything here is __host__ __device__ so the same source runs in the
+// sm_103a kernels and in host-side unit tests.  It evaluates the Cosserat rod
+// strains of the reference (src/cuda_backend.cu:234-245), their energy, the
+// gradient and the Gauss-Newton Hessian blocks (src/cuda_backend.cu:899-919)
+// with closed-form derivatives of the SO(3) exponential (left Jacobian)
+// and of the regularised Cayley map instead of the reference's Dual<12>
+// forward-mode AD, plus the log-barrier contact term
+// (src/cuda_backend.cu:255-265, 920-938) and the device segment-triangle
+// distance (src/cuda_backend.cu:200-223).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define KHS_HD __host__ __device__ __forceinline__
+#else
+#define KHS_HD inline
+#endif
+
+namespace khs {
+namespace dm {
+
+constexpr double kPi = 3.1415926535897932384626433832795;
+
+struct V {
+    double x, y, z;
+};
+
+KHS_HD V v(double x, double y, double z) { V r; r.x = x; r.y = y; r.z = z; return r; }
+KHS_HD V operator+(V a, V b) { return v(a.x + b.x, a.y + b.y, a.z + b.z); }
+KHS_HD V operator-(V a, V b) { return v(a.x - b.x, a.y - b.y, a.z - b.z); }
+KHS_HD V operator*(V a, double s) { return v(a.x * s, a.y * s, a.z * s); }
+KHS_HD double dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+KHS_HD V cross(V a, V b) { return v(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+KHS_HD double norm(V a) { return sqrt(dot(a, a)); }
+KHS_HD V vmin(V a, V b) { return v(fmin(a.x, b.x), fmin(a.y, b.y), fmin(a.z, b.z)); }
+KHS_HD V vmax(V a, V b) { return v(fmax(a.x, b.x), fmax(a.y, b.y), fmax(a.z, b.z)); }
+KHS_HD double at(V a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+// 3x3 row-major.
+struct M {
+    double m[9];
+};
+
+KHS_HD M mmul(const M &a, const M &b)
+{
+    M r;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r.m[3 * i + j] = a.m[3 * i] * b.m[j] + a.m[3 * i + 1] * b.m[3 + j] + a.m[3 * i + 2] * b.m[6 + j];
+    return r;
+}
+// a^T b
+KHS_HD M mtmul(const M &a, const M &b)
+{
+    M r;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r.m[3 * i + j] = a.m[i] * b.m[j] + a.m[3 + i] * b.m[3 + j] + a.m[6 + i] * b.m[6 + j];
+    return r;
+}
+// a^T x
+KHS_HD V mtvec(const M &a, V x)
+{
+    return v(a.m[0] * x.x + a.m[3] * x.y + a.m[6] * x.z, a.m[1] * x.x + a.m[4] * x.y + a.m[7] * x.z,
+             a.m[2] * x.x + a.m[5] * x.y + a.m[8] * x.z);
+}
+KHS_HD V mvec(const M &a, V x)
+{
+    return v(a.m[0] * x.x + a.m[1] * x.y + a.m[2] * x.z, a.m[3] * x.x + a.m[4] * x.y + a.m[5] * x.z,
+             a.m[6] * x.x + a.m[7] * x.y + a.m[8] * x.z);
+}
+
+// Rotation R = exp([u]x) Ref with the reference's Rodrigues coefficients and
+// small-angle Taylor branch below theta^2 = 1e-10 (cuda_backend.cu:130-136).
+// Also returns the left Jacobian Jl(u), defined by
+// exp(u + du) = exp([Jl du]x) exp(u) + O(du^2), as I + p W + r W^2 with
+// p = 2 sin^2(t/2) / t^2 (cancellation-free form of (1 - cos t) / t^2) and
+// r = (t - sin t) / t^3, both from their Taylor series below t^2 = 1e-4.
+KHS_HD void rotation_and_jacobian(V u, const double *ref, M &R, M *Jl)
+{
+    const double t2 = dot(u, u);
+    double a, b;
+    double s, c;
+    if (t2 < 1.0e-10) {
+        a = 1.0 - t2 / 6.0 + t2 * t2 / 120.0;
+        b = 0.5 - t2 / 24.0 + t2 * t2 / 720.0;
+        s = 0.0; c = 1.0;
+    } else {
+        const double t = sqrt(t2);
+        sincos(t, &s, &c);
+        a = s / t;
+        b = (1.0 - c) / t2;
+    }
+    // E = I + a W + b W^2 with W = [u]x.
+    const double wx = u.x, wy = u.y, wz = u.z;
+    const double w2[9] = {-(wy * wy + wz * wz), wx * wy, wx * wz,
+                          wx * wy, -(wx * wx + wz * wz), wy * wz,
+                          wx * wz, wy * wz, -(wx * wx + wy * wy)};
+    M E;
+    E.m[0] = 1.0 + b * w2[0]; E.m[1] = -a * wz + b * w2[1]; E.m[2] = a * wy + b * w2[2];
+    E.m[3] = a * wz + b * w2[3]; E.m[4] = 1.0 + b * w2[4]; E.m[5] = -a * wx + b * w2[5];
+    E.m[6] = -a * wy + b * w2[6]; E.m[7] = a * wx + b * w2[7]; E.m[8] = 1.0 + b * w2[8];
+    M Rf;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Rf.m[k] = ref[k];
+    R = mmul(E, Rf);
+    if (Jl) {
+        double p, r;  // Jl = I + p W + r W^2
+        if (t2 < 1.0e-4) {
+            p = 0.5 - t2 / 24.0 + t2 * t2 / 720.0 - t2 * t2 * t2 / 40320.0;
+            r = 1.0 / 6.0 - t2 / 120.0 + t2 * t2 / 5040.0 - t2 * t2 * t2 / 362880.0;
+        } else {
+            const double t = sqrt(t2);
+            const double sh = sin(0.5 * t);
+            p = 2.0 * sh * sh / t2;
+            r = (t - s) / (t2 * t);
+        }
+        M &J = *Jl;
+        J.m[0] = 1.0 + r * w2[0]; J.m[1] = -p * wz + r * w2[1]; J.m[2] = p * wy + r * w2[2];
+        J.m[3] = p * wz + r * w2[3]; J.m[4] = 1.0 + r * w2[4]; J.m[5] = -p * wx + r * w2[5];
+        J.m[6] = -p * wy + r * w2[6]; J.m[7] = p * wx + r * w2[7]; J.m[8] = 1.0 + r * w2[8];
+    }
+}
+
+// Material weights of the six strains (cuda_backend.cu:905-907):
+// shear, shear, stretch, bend, bend, twist.
+struct Weights {
+    double w[6];
+};
+
+KHS_HD Weights strain_weights(double radius, double young, double poisson, double shear_correction)
+{
+    const double area = kPi * radius * radius;
+    const double inertia = kPi * radius * radius * radius * radius / 4.0;
+    const double G = young / (2.0 * (1.0 + poisson));
+    Weights r;
+    r.w[0] = shear_correction * G * area;
+    r.w[1] = r.w[0];
+    r.w[2] = young * area;
+    r.w[3] = young * inertia;
+    r.w[4] = r.w[3];
+    r.w[5] = 2.0 * G * inertia;
+    return r;
+}
+
+// Strain of one element and, optionally, its Jacobian.
+//   gamma = 0.5 (Ri^T + Rj^T) t - gamma0,    t = (xj - xi) / L0
+//   kappa = cay(Ri^T Rj) / L0 - kappa0
+// Jacobian (per 3x3 block; [.]x = cross-product matrix):
+//   d gamma / d xj = -d gamma / d xi = A = 0.5 (Ri^T + Rj^T) / L0
+//   d gamma / d ui = 0.5 Ri^T [t]x Jl(ui),  d gamma / d uj = 0.5 Rj^T [t]x Jl(uj)
+//   d kappa / d uj = -d kappa / d ui|_(Jl(ui) -> Jl(uj)) = K Ri^T Jl(uj) / L0
+//   with K = ((tr Q) I - Q) / s + 2 c c^T / s^2, Q = Ri^T Rj, c = axial(Q),
+//   s = 1 + (tr Q - 1) / 2 + 1e-12 (differential of the regularised Cayley
+//   map along dQ = [w]x Q).
+struct ElementJacobian {
+    M A, Sgi, Sgj, Kki, Kkj;
+};
+
+KHS_HD void element_strain(const M &Ri, const M &Rj, V xi, V xj, double L0, V gamma0, V kappa0, double eps[6],
+                           ElementJacobian *J, const M *Jli, const M *Jlj)
+{
+    const double invL = 1.0 / L0;
+    const V t = (xj - xi) * invL;
+    M S;  // Ri^T + Rj^T
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S.m[3 * r + c] = Ri.m[3 * c + r] + Rj.m[3 * c + r];
+    const V shear = mvec(S, t) * 0.5;
+    const M Q = mtmul(Ri, Rj);
+    const V ax = v((Q.m[7] - Q.m[5]) * 0.5, (Q.m[2] - Q.m[6]) * 0.5, (Q.m[3] - Q.m[1]) * 0.5);
+    const double trQ = Q.m[0] + Q.m[4] + Q.m[8];
+    const double s = 1.0 + (trQ - 1.0) * 0.5 + 1.0e-12;
+    const double f = 2.0 / s;
+    eps[0] = shear.x - gamma0.x;
+    eps[1] = shear.y - gamma0.y;
+    eps[2] = shear.z - gamma0.z;
+    eps[3] = ax.x * f * invL - kappa0.x;
+    eps[4] = ax.y * f * invL - kappa0.y;
+    eps[5] = ax.z * f * invL - kappa0.z;
+    if (!J) return;
+    // A = 0.5 (Ri + Rj)^T / L0
+    const double hl = 0.5 * invL;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) J->A.m[k] = S.m[k] * hl;
+    // [t]x Jl: column k = t x Jl_col(k)
+    M TJi, TJj;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const V ci = cross(t, v(Jli->m[k], Jli->m[3 + k], Jli->m[6 + k]));
+        const V cj = cross(t, v(Jlj->m[k], Jlj->m[3 + k], Jlj->m[6 + k]));
+        TJi.m[k] = ci.x; TJi.m[3 + k] = ci.y; TJi.m[6 + k] = ci.z;
+        TJj.m[k] = cj.x; TJj.m[3 + k] = cj.y; TJj.m[6 + k] = cj.z;
+    }
+    J->Sgi = mtmul(Ri, TJi);
+    J->Sgj = mtmul(Rj, TJj);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { J->Sgi.m[k] *= 0.5; J->Sgj.m[k] *= 0.5; }
+    // K
+    M K;
+    const double is = 1.0 / s, is2 = 2.0 * is * is;
+    const double axv[3] = {ax.x, ax.y, ax.z};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) K.m[3 * r + c] = ((r == c ? trQ : 0.0) - Q.m[3 * r + c]) * is + is2 * axv[r] * axv[c];
+    const M RJi = mtmul(Ri, *Jli), RJj = mtmul(Ri, *Jlj);
+    J->Kki = mmul(K, RJi);
+    J->Kkj = mmul(K, RJj);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { J->Kki.m[k] *= -invL; J->Kkj.m[k] *= invL; }
+}
+
+// Elastic energy 0.5 L0 sum w eps^2.
+KHS_HD double element_energy(const double eps[6], const Weights &w, double L0)
+{
+    double e = 0.0;
+#pragma unroll
+    for (int s = 0; s < 6; ++s) e += (0.5 * L0 * w.w[s]) * eps[s] * eps[s];
+    return e;
+}
+
+// Gradient of the element energy: gi, gj (6 each; translation then
+// rotation) = L0 J^T diag(w) eps.
+KHS_HD void element_gradient(const ElementJacobian &J, const double eps[6], const Weights &w, double L0, double gi[6],
+                             double gj[6])
+{
+    double se[3], ke[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { se[k] = L0 * w.w[k] * eps[k]; ke[k] = L0 * w.w[3 + k] * eps[3 + k]; }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double ax = J.A.m[c] * se[0] + J.A.m[3 + c] * se[1] + J.A.m[6 + c] * se[2];
+        gi[c] = -ax;
+        gj[c] = ax;
+        gi[3 + c] = J.Sgi.m[c] * se[0] + J.Sgi.m[3 + c] * se[1] + J.Sgi.m[6 + c] * se[2] +
+                    J.Kki.m[c] * ke[0] + J.Kki.m[3 + c] * ke[1] + J.Kki.m[6 + c] * ke[2];
+        gj[3 + c] = J.Sgj.m[c] * se[0] + J.Sgj.m[3 + c] * se[1] + J.Sgj.m[6 + c] * se[2] +
+                    J.Kkj.m[c] * ke[0] + J.Kkj.m[3 + c] * ke[1] + J.Kkj.m[6 + c] * ke[2];
+    }
+}
+
+// X^T diag(d) Y for 3x3 X, Y.
+KHS_HD void xtdy(const M &X, const double d[3], const M &Y, double *out, int ld, bool accumulate, double sign)
+{
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double h = X.m[r] * d[0] * Y.m[c] + X.m[3 + r] * d[1] * Y.m[3 + c] + X.m[6 + r] * d[2] * Y.m[6 + c];
+            if (accumulate) out[ld * r + c] += sign * h;
+            else out[ld * r + c] = sign * h;
+        }
+}
+
+// Gauss-Newton Hessian blocks L0 J^T diag(w) J of one element, as 6x6
+// row-major blocks: Hii, Hjj (diagonal blocks of the two nodes) and Hij
+// (rows of node i, columns of node j).
+KHS_HD void element_hessian(const ElementJacobian &J, const Weights &w, double L0, double *Hii, double *Hjj, double *Hij)
+{
+    const double dg[3] = {L0 * w.w[0], L0 * w.w[1], L0 * w.w[2]};
+    const double dk[3] = {L0 * w.w[3], L0 * w.w[4], L0 * w.w[5]};
+    // translation-translation: A^T Wg A (with signs -,+ for i,j)
+    xtdy(J.A, dg, J.A, Hii, 6, false, 1.0);
+    xtdy(J.A, dg, J.A, Hjj, 6, false, 1.0);
+    xtdy(J.A, dg, J.A, Hij, 6, false, -1.0);
+    // translation-rotation
+    xtdy(J.A, dg, J.Sgi, Hii + 3, 6, false, -1.0);   // xi,ui
+    xtdy(J.Sgi, dg, J.A, Hii + 18, 6, false, -1.0);  // ui,xi
+    xtdy(J.A, dg, J.Sgj, Hjj + 3, 6, false, 1.0);    // xj,uj
+    xtdy(J.Sgj, dg, J.A, Hjj + 18, 6, false, 1.0);   // uj,xj
+    xtdy(J.A, dg, J.Sgj, Hij + 3, 6, false, -1.0);   // xi,uj
+    xtdy(J.Sgi, dg, J.A, Hij + 18, 6, false, 1.0);   // ui,xj
+    // rotation-rotation
+    xtdy(J.Sgi, dg, J.Sgi, Hii + 21, 6, false, 1.0);
+    xtdy(J.Kki, dk, J.Kki, Hii + 21, 6, true, 1.0);
+    xtdy(J.Sgj, dg, J.Sgj, Hjj + 21, 6, false, 1.0);
+    xtdy(J.Kkj, dk, J.Kkj, Hjj + 21, 6, true, 1.0);
+    xtdy(J.Sgi, dg, J.Sgj, Hij + 21, 6, false, 1.0);
+    xtdy(J.Kki, dk, J.Kkj, Hij + 21, 6, true, 1.0);
+}
+
+// ---- geometry (device flavour, cuda_backend.cu:200-223) ----------------
+//
+// The proximity tests decide integer outputs (candidate sets, closest
+// triangle, active flags), so they are evaluated without FMA contraction:
+// every product and sum is rounded on its own (__dmul_rn / __dadd_rn on the
+// device, plain operations in host code built with -ffp-contract=off).
+// Given the same inputs the device then produces the same bits as a
+// correctly rounded host evaluation, including exact-distance ties.
+
+#if defined(__CUDA_ARCH__)
+KHS_HD double xm(double a, double b) { return __dmul_rn(a, b); }
+KHS_HD double xa(double a, double b) { return __dadd_rn(a, b); }
+KHS_HD double xs(double a, double b) { return __dsub_rn(a, b); }
+#else
+KHS_HD double xm(double a, double b) { return a * b; }
+KHS_HD double xa(double a, double b) { return a + b; }
+KHS_HD double xs(double a, double b) { return a - b; }
+#endif
+KHS_HD V gadd(V a, V b) { return v(xa(a.x, b.x), xa(a.y, b.y), xa(a.z, b.z)); }
+KHS_HD V gsub(V a, V b) { return v(xs(a.x, b.x), xs(a.y, b.y), xs(a.z, b.z)); }
+KHS_HD V gmul(V a, double s) { return v(xm(a.x, s), xm(a.y, s), xm(a.z, s)); }
+KHS_HD double gdot(V a, V b) { return xa(xa(xm(a.x, b.x), xm(a.y, b.y)), xm(a.z, b.z)); }
+KHS_HD double gnorm(V a) { return sqrt(gdot(a, a)); }
+
+struct ClosestPair {
+    double distance, t;
+    V bary;
+};
+
+KHS_HD V closest_point_triangle(V p, V a, V b, V c, V &bary)
+{
+    const V ab = gsub(b, a), ac = gsub(c, a), ap = gsub(p, a);
+    const double d1 = gdot(ab, ap), d2 = gdot(ac, ap);
+    if (d1 <= 0 && d2 <= 0) { bary = v(1, 0, 0); return a; }
+    const V bp = gsub(p, b);
+    const double d3 = gdot(ab, bp), d4 = gdot(ac, bp);
+    if (d3 >= 0 && d4 <= d3) { bary = v(0, 1, 0); return b; }
+    const double vc = xs(xm(d1, d4), xm(d3, d2));
+    if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+        const double w = d1 / xs(d1, d3);
+        bary = v(xs(1.0, w), w, 0);
+        return gadd(a, gmul(ab, w));
+    }
+    const V cp = gsub(p, c);
+    const double d5 = gdot(ab, cp), d6 = gdot(ac, cp);
+    if (d6 >= 0 && d5 <= d6) { bary = v(0, 0, 1); return c; }
+    const double vb = xs(xm(d5, d2), xm(d1, d6));
+    if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+        const double w = d2 / xs(d2, d6);
+        bary = v(xs(1.0, w), 0, w);
+        return gadd(a, gmul(ac, w));
+    }
+    const double va = xs(xm(d3, d6), xm(d5, d4));
+    if (va <= 0 && xs(d4, d3) >= 0 && xs(d5, d6) >= 0) {
+        const double w = xs(d4, d3) / xa(xs(d4, d3), xs(d5, d6));
+        bary = v(0, xs(1.0, w), w);
+        return gadd(b, gmul(gsub(c, b), w));
+    }
+    const double inv = 1.0 / xa(xa(va, vb), vc), vv = xm(vb, inv), ww = xm(vc, inv);
+    bary = v(xs(xs(1.0, vv), ww), vv, ww);
+    return gadd(gadd(a, gmul(ab, vv)), gmul(ac, ww));
+}
+
+KHS_HD void segment_segment_params(V p1, V q1, V p2, V q2, double &s, double &t)
+{
+    const V d1 = gsub(q1, p1), d2 = gsub(q2, p2), r = gsub(p1, p2);
+    const double a = gdot(d1, d1), e = gdot(d2, d2), f = gdot(d2, r);
+    s = 0.0; t = 0.0;
+    if (a <= 1e-14 && e <= 1e-14) return;
+    if (a <= 1e-14) { t = fmin(1.0, fmax(0.0, f / e)); return; }
+    const double c = gdot(d1, r);
+    if (e <= 1e-14) { s = fmin(1.0, fmax(0.0, -c / a)); return; }
+    const double b = gdot(d1, d2), den = xs(xm(a, e), xm(b, b));
+    if (den != 0) s = fmin(1.0, fmax(0.0, xs(xm(b, f), xm(c, e)) / den));
+    t = xa(xm(b, s), f) / e;
+    if (t < 0) { t = 0; s = fmin(1.0, fmax(0.0, -c / a)); }
+    else if (t > 1) { t = 1; s = fmin(1.0, fmax(0.0, xs(b, c) / a)); }
+}
+
+// Closest pair between segment p0-p1 and triangle abc: end points against
+// the face, then the segment against the three edges, keeping the first
+// strictly smaller distance.  No interior-crossing test (device semantics of
+// the reference).
+KHS_HD ClosestPair closest_segment_triangle(V p0, V p1, V a, V b, V c)
+{
+    ClosestPair out;
+    out.distance = 1.0e300; out.t = 0.0; out.bary = v(1, 0, 0);
+    V bary;
+    V cp = closest_point_triangle(p0, a, b, c, bary);
+    double d = gnorm(gsub(p0, cp));
+    if (d < out.distance) { out.distance = d; out.t = 0.0; out.bary = bary; }
+    cp = closest_point_triangle(p1, a, b, c, bary);
+    d = gnorm(gsub(p1, cp));
+    if (d < out.distance) { out.distance = d; out.t = 1.0; out.bary = bary; }
+    const V d1 = gsub(p1, p0);
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const V p2 = e == 0 ? a : (e == 1 ? b : c);
+        const V q2 = e == 0 ? b : (e == 1 ? c : a);
+        double s, t;
+        segment_segment_params(p0, p1, p2, q2, s, t);
+        const double dd = gnorm(gsub(gadd(p0, gmul(d1, s)), gadd(p2, gmul(gsub(q2, p2), t))));
+        if (dd < out.distance) {
+            out.distance = dd;
+            out.t = s;
+            if (e == 0) out.bary = v(xs(1.0, t), t, 0);
+            else if (e == 1) out.bary = v(0, xs(1.0, t), t);
+            else out.bary = v(t, 0, xs(1.0, t));
+        }
+    }
+    return out;
+}
+
+KHS_HD bool boxes_overlap(V al, V au, V bl, V bu, double p)
+{
+    return al.x <= bu.x + p && bl.x <= au.x + p && al.y <= bu.y + p && bl.y <= au.y + p && al.z <= bu.z + p &&
+           bl.z <= au.z + p;
+}
+
+// Log barrier b(g) = -kc (dh - g)^2 ln(g / dh) of the contact gap and its
+// gradient with respect to the two segment end points at fixed (t, bary)
+// (cuda_backend.cu:255-265: the distance is regularised by 1e-30 inside the
+// square root).  Returns the energy; g0, g1 get the gradients.
+KHS_HD double barrier_energy_gradient(V x0, V x1, double t, V body_point, double radius_offset, double dh, double kc,
+                                      double g0[3], double g1[3])
+{
+    const V p = x0 * (1.0 - t) + x1 * t;
+    const V diff = p - body_point;
+    const double dist = sqrt(dot(diff, diff) + 1e-30);
+    const double gap = dist - radius_offset;
+    if (gap >= dh) {
+        g0[0] = g0[1] = g0[2] = g1[0] = g1[1] = g1[2] = 0.0;
+        return 0.0;
+    }
+    const double aa = dh - gap, lg = log(gap / dh);
+    const double energy = -kc * aa * aa * lg;
+    const double db = kc * (2.0 * aa * lg - aa * aa / gap);  // d energy / d gap
+    const double s = db / dist;
+    g0[0] = s * diff.x * (1.0 - t); g0[1] = s * diff.y * (1.0 - t); g0[2] = s * diff.z * (1.0 - t);
+    g1[0] = s * diff.x * t; g1[1] = s * diff.y * t; g1[2] = s * diff.z * t;
+    return energy;
+}
+
+}  // namespace dm
+}  // namespace khs

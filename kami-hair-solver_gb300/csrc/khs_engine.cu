@@ -1,0 +1,1884 @@
+// GB300 device engine (see khs_engine.hpp).
+//
+// Device data layout (one arena allocation, 256-byte aligned sub-arrays):
+//   node state     q, q_old, v, q_snap, v_snap, q_base   [N][6] FP64
+//   solver vectors grad, dir, precond, dprime            [N][6] FP64
+//   block matrices diag, upper, cprime                   [N][36] FP64
+//   rotation cache R = exp(u) Ref, left Jacobian Jl      [N][9] FP64
+//   element parts  contributions of the element whose left node is n
+//                  (as_i_*) and whose right node is n (as_j_*) so every
+//                  node sums its two incident elements in a fixed order
+//                  without atomics
+//   elements       (i, j, contact flag, L0, gamma0, kappa0), energies,
+//                  contact records                        [E]
+//   strands        first, count, fixed prefix, length-sorted order [S]
+//   collider       triangles [T][3], current/old/frame-start/pending
+//                  vertices [V][3], BVH in right-first preorder with escape
+//                  indices (stackless traversal) and parent links (one-launch
+//                  bottom-up refit)
+//
+// Kernels (one thread per node / element / strand / BVH leaf):
+//   k_begin_substep, k_collider_interp, k_refit, k_sweep(+record),
+//   k_precond, k_node_eval, k_elem_eval, k_node_sum, k_reduce_eval,
+//   k_final_eval, k_block_solve, k_steepest, k_scale, k_reduce_dir,
+//   k_final_dir, k_ccd, k_update_velocity, k_friction, k_friction_apply,
+//   k_gather.  Reductions are two-level (fixed per-block trees, then one
+//   block over the partials) and therefore deterministic.
+#include "khs_engine.hpp"
+#include "khs_device_math.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <stdexcept>
+
+namespace khs {
+namespace {
+
+#define KHS_CUDA(call)                                                                         \
+    do {                                                                                       \
+        const cudaError_t khs_err = (call);                                                    \
+        if (khs_err != cudaSuccess) throw std::runtime_error(std::string("CUDA: ") + cudaGetErrorString(khs_err)); \
+    } while (0)
+
+using dm::V;
+using dm::M;
+
+constexpr int kBlock = 256;
+constexpr int kPartials = 304;  // 2 reduction blocks per SM on a 152-SM GB300
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr uint64_t kCheckpointMagic = 0x3154504348534bULL;  // same blob header as the reference
+constexpr uint8_t kFlagActive = 1, kFlagInfeasible = 2, kFlagEnergy = 4, kFlagClosest = 8;
+
+inline unsigned grid_for(size_t n) { return unsigned((n + kBlock - 1) / kBlock); }
+
+// Scalars produced by one evaluation / direction pass (host-mapped).
+struct Mailbox {
+    double objective, elastic, contact, kinetic, minimum_gap, grad_norm2;
+    unsigned long long candidates, active;
+    int feasible;
+    int solve_failed;
+    double slope, dir_norm2, max_translation;
+    unsigned long long ccd_bits;
+    uint32_t sweep_fail;
+    uint32_t pad;
+};
+
+// Atomic targets live in device memory; the publishing kernels copy them to
+// the host-mapped mailbox and reset them for the next use.
+struct Scalars {
+    unsigned long long ccd_bits;
+    uint32_t sweep_fail;
+    int solve_failed;
+};
+
+struct Partial {
+    double node_energy, kinetic, elastic, contact, min_gap, grad2;
+    unsigned long long candidates, active;
+    int infeasible;
+    int pad;
+};
+
+struct DirPartial {
+    double slope, dnorm2, max_translation;
+};
+
+struct SweepRecord {
+    uint32_t claimed, strand, element, triangle;
+    double distance, required, clearance, displacement;
+    double hair_start[3], hair_end[3], collider_point[3];
+};
+
+// POD view of every device array (passed by value to kernels).
+struct View {
+    uint32_t N, E, S, V, T, B;
+    double *q, *q_old, *v, *q_base, *grad, *dir, *precond;
+    double *rot, *jl, *node_energy, *node_kinetic;
+    double *diag, *upper, *cprime, *dprime;
+    double *as_i_g, *as_j_g, *as_i_h, *as_j_h, *as_i_f, *as_j_f;
+    const double *ref, *mass, *rmass;
+    const uint8_t *fixed;
+    const int32_t *elem_left, *elem_right;
+    const uint32_t *ei, *ej, *estrand;
+    const uint8_t *econtact;
+    const double *L0, *gamma0, *kappa0;
+    double *e_el, *e_co, *c_gap;
+    uint32_t *c_cand, *c_tri;
+    uint8_t *c_flags;
+    const uint32_t *sfirst, *scount, *sfixed, *sorder;
+    const uint32_t *tri;
+    double *col_cur, *col_old;
+    double *blo, *bhi;
+    const uint32_t *besc, *bfirst, *bcount, *border, *bleaves;
+    const int32_t *bparent;
+    const uint32_t *bleft, *bright;
+    uint32_t *brefit;
+    uint32_t L;
+    Partial *partials;
+    DirPartial *dpartials;
+    Scalars *sc;          // device
+    Mailbox *mail;        // host-mapped
+    SweepRecord *sweep;   // host-mapped
+    // material / desc
+    double radius, offset, dhat, kc, friction, smoothing, damping, min_gap;
+    double gx, gy, gz;
+    dm::Weights w;
+    double young, poisson, shear_corr;
+    int has_collider;
+};
+
+__device__ __forceinline__ V load3(const double *p) { return dm::v(p[0], p[1], p[2]); }
+__device__ __forceinline__ void store3(double *p, V a) { p[0] = a.x; p[1] = a.y; p[2] = a.z; }
+__device__ __forceinline__ M load9(const double *p)
+{
+    M r;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) r.m[k] = p[k];
+    return r;
+}
+__device__ __forceinline__ V tri_vertex(const View &d, uint32_t t, int c) { return load3(d.col_cur + 3 * size_t(d.tri[3 * t + c])); }
+
+// Stackless BVH walk in the reference's visiting order.
+template<class F> __device__ void bvh_query(const View &d, V lo, V hi, double pad, F &&f)
+{
+    uint32_t i = 0;
+    while (i < d.B) {
+        const V nl = load3(d.blo + 3 * size_t(i)), nh = load3(d.bhi + 3 * size_t(i));
+        if (!dm::boxes_overlap(lo, hi, nl, nh, pad)) { i = d.besc[i]; continue; }
+        const uint32_t cnt = d.bcount[i];
+        if (cnt == 0) { ++i; continue; }
+        const uint32_t first = d.bfirst[i];
+        for (uint32_t k = first; k < first + cnt; ++k) f(d.border[k]);
+        i = d.besc[i];
+    }
+}
+
+// ---- per-substep set-up ---------------------------------------------------
+
+__global__ void __launch_bounds__(kBlock) k_begin_substep(View d, const double *root_a, const double *rot_a,
+                                                          const double *root_b, const double *rot_b, double f, double dt)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    double q[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { q[k] = d.q[6 * size_t(n) + k]; d.q_old[6 * size_t(n) + k] = q[k]; }
+    if (!d.fixed[n]) return;
+    // Uncontracted lerps: the root targets and collider vertices feed the
+    // integer contact work, so they round exactly like a host evaluation.
+    const V p = dm::gadd(dm::gmul(load3(root_a + 3 * size_t(n)), 1.0 - f), dm::gmul(load3(root_b + 3 * size_t(n)), f));
+    const V r = dm::gadd(dm::gmul(load3(rot_a + 3 * size_t(n)), 1.0 - f), dm::gmul(load3(rot_b + 3 * size_t(n)), f));
+    const double vals[6] = {p.x, p.y, p.z, r.x, r.y, r.z};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        d.q[6 * size_t(n) + k] = vals[k];
+        d.v[6 * size_t(n) + k] = (vals[k] - q[k]) / dt;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_collider_interp(View d, const double *a, const double *b, double f)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.V) return;
+    const V cur = load3(d.col_cur + 3 * size_t(i));
+    store3(d.col_old + 3 * size_t(i), cur);
+    store3(d.col_cur + 3 * size_t(i), dm::gadd(dm::gmul(load3(a + 3 * size_t(i)), 1.0 - f), dm::gmul(load3(b + 3 * size_t(i)), f)));
+}
+
+// Bottom-up refit in one launch: each leaf thread computes its box and walks
+// up; the second child to arrive at a parent (atomic counter) merges the two
+// children, resets the counter for the next launch and continues.
+__global__ void __launch_bounds__(kBlock) k_refit(View d, int swept)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.L) return;
+    uint32_t node = d.bleaves[k];
+    V lo = dm::v(1e300, 1e300, 1e300), hi = dm::v(-1e300, -1e300, -1e300);
+    const uint32_t first = d.bfirst[node], cnt = d.bcount[node];
+    for (uint32_t j = first; j < first + cnt; ++j) {
+        const uint32_t t = d.border[j];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const uint32_t vi = d.tri[3 * t + c];
+            const V a = load3(d.col_cur + 3 * size_t(vi));
+            lo = dm::vmin(lo, a); hi = dm::vmax(hi, a);
+            if (swept) { const V o = load3(d.col_old + 3 * size_t(vi)); lo = dm::vmin(lo, o); hi = dm::vmax(hi, o); }
+        }
+    }
+    store3(d.blo + 3 * size_t(node), lo);
+    store3(d.bhi + 3 * size_t(node), hi);
+    for (;;) {
+        const int32_t p = d.bparent[node];
+        if (p < 0) return;
+        __threadfence();
+        if (atomicAdd(&d.brefit[p], 1u) == 0) return;
+        d.brefit[p] = 0;
+        __threadfence();
+        const volatile double *blo = d.blo, *bhi = d.bhi;
+        const uint32_t l = d.bleft[p], r = d.bright[p];
+        const V llo = dm::v(blo[3 * l], blo[3 * l + 1], blo[3 * l + 2]), rlo = dm::v(blo[3 * r], blo[3 * r + 1], blo[3 * r + 2]);
+        const V lhi = dm::v(bhi[3 * l], bhi[3 * l + 1], bhi[3 * l + 2]), rhi = dm::v(bhi[3 * r], bhi[3 * r + 1], bhi[3 * r + 2]);
+        store3(d.blo + 3 * size_t(p), dm::vmin(llo, rlo));
+        store3(d.bhi + 3 * size_t(p), dm::vmax(lhi, rhi));
+        node = uint32_t(p);
+    }
+}
+
+// Conservative advancement of each moving triangle against the stationary
+// hair at the start of the substep (cuda_backend.cu:975-987).  Returns the
+// first failing triangle of this element in traversal order.
+__device__ bool sweep_element(const View &d, uint32_t e, SweepRecord *rec)
+{
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
+    const double target = d.radius + d.offset + d.min_gap;
+    bool failed = false;
+    bvh_query(d, dm::vmin(p0, p1), dm::vmax(p0, p1), target, [&](uint32_t t) {
+        if (failed) return;
+        const V oa = load3(d.col_old + 3 * size_t(d.tri[3 * t])), ob = load3(d.col_old + 3 * size_t(d.tri[3 * t + 1])),
+                oc = load3(d.col_old + 3 * size_t(d.tri[3 * t + 2]));
+        const V da = dm::gsub(tri_vertex(d, t, 0), oa), db = dm::gsub(tri_vertex(d, t, 1), ob),
+                dc = dm::gsub(tri_vertex(d, t, 2), oc);
+        const double speed = fmax(dm::gnorm(da), fmax(dm::gnorm(db), dm::gnorm(dc)));
+        if (speed < 1e-30) return;
+        double alpha = 0.0;
+        bool end = false;
+        dm::ClosestPair pair;
+        V a, b, c;
+        for (int k = 0; k < 80; ++k) {
+            a = dm::gadd(oa, dm::gmul(da, alpha)); b = dm::gadd(ob, dm::gmul(db, alpha)); c = dm::gadd(oc, dm::gmul(dc, alpha));
+            pair = dm::closest_segment_triangle(p0, p1, a, b, c);
+            const double clearance = pair.distance - target;
+            if (clearance <= 0) { failed = true; break; }
+            const double advance = 0.8 * clearance / speed;
+            if (alpha + advance >= 1) { end = true; break; }
+            if (advance < 1e-12) { failed = true; break; }
+            alpha += advance;
+        }
+        if (!end) failed = true;
+        if (failed && rec) {
+            rec->claimed = 1; rec->strand = d.estrand[e]; rec->element = e; rec->triangle = t;
+            rec->distance = pair.distance; rec->required = target; rec->clearance = pair.distance - target;
+            rec->displacement = speed;
+            store3(rec->hair_start, p0); store3(rec->hair_end, p1);
+            store3(rec->collider_point, dm::gadd(dm::gadd(dm::gmul(a, pair.bary.x), dm::gmul(b, pair.bary.y)), dm::gmul(c, pair.bary.z)));
+        }
+    });
+    return failed;
+}
+
+__global__ void __launch_bounds__(kBlock) k_sweep(View d)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    if (d.fixed[d.ei[e]] || !d.econtact[e]) return;
+    if (sweep_element(d, e, nullptr)) atomicMin(&d.sc->sweep_fail, e);
+}
+
+// Publishes the lowest failing element of k_sweep (with its first failing
+// triangle in traversal order) and re-arms the atomic.
+__global__ void k_sweep_record(View d)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    const uint32_t e = d.sc->sweep_fail;
+    d.sc->sweep_fail = kNone;
+    d.mail->sweep_fail = e;
+    if (e == kNone) return;
+    SweepRecord rec{};
+    sweep_element(d, e, &rec);
+    *d.sweep = rec;
+}
+
+// Diagonal preconditioner (cuda_backend.cu:815-841): node term then the
+// left and right incident elements, inverted; 0 at fixed nodes.
+__global__ void __launch_bounds__(kBlock) k_precond(View d, double dt)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    const double inv = 1.0 / dt, inv2 = inv * inv;
+    double t = d.mass[n] * (inv2 + d.damping * inv), r = d.rmass[n] * (inv2 + d.damping * inv);
+    const double area = dm::kPi * d.radius * d.radius;
+    const double inertia = dm::kPi * d.radius * d.radius * d.radius * d.radius / 4.0;
+    const double G = d.young / (2.0 * (1.0 + d.poisson));
+    const int32_t es[2] = {d.elem_left[n], d.elem_right[n]};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (es[k] < 0) continue;
+        const double L = d.L0[es[k]];
+        t += fmax(d.young * area, d.shear_corr * G * area) / L;
+        r += d.shear_corr * G * area * L + fmax(d.young * inertia, 2.0 * G * inertia) / L;
+    }
+    const bool fx = d.fixed[n];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        d.precond[6 * size_t(n) + k] = fx ? 0.0 : 1.0 / fmax(t, 1.0e-30);
+        d.precond[6 * size_t(n) + 3 + k] = fx ? 0.0 : 1.0 / fmax(r, 1.0e-30);
+    }
+}
+
+// ---- energy / gradient / Gauss-Newton Hessian -----------------------------
+
+// Per node: optional line-search update q = q_base + alpha dir, rotation
+// cache, inertia + damping energy, gradient and diagonal
+// (cuda_backend.cu:883-897).
+__global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int trial, double alpha, double dt)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    double q[6];
+    const size_t o = 6 * size_t(n);
+    if (trial) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { q[k] = d.q_base[o + k] + alpha * d.dir[o + k]; d.q[o + k] = q[k]; }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[k] = d.q[o + k];
+    }
+    M R, J;
+    dm::rotation_and_jacobian(dm::v(q[3], q[4], q[5]), d.ref + 9 * size_t(n), R, gradient ? &J : nullptr);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) d.rot[9 * size_t(n) + k] = R.m[k];
+    if (gradient) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) d.jl[9 * size_t(n) + k] = J.m[k];
+        for (int k = 0; k < 36; ++k) d.diag[36 * size_t(n) + k] = 0.0;
+    }
+    if (d.fixed[n]) {
+        d.node_energy[n] = 0.0;
+        d.node_kinetic[n] = 0.0;
+        if (gradient) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) d.grad[o + k] = 0.0;
+        }
+        return;
+    }
+    const double inv = 1.0 / dt, inv2 = inv * inv, m = d.mass[n], mr = d.rmass[n];
+    const double kx = m * inv2, kr = mr * inv2, cx = m * d.damping * inv, cr = mr * d.damping * inv;
+    const double grav[3] = {d.gx, d.gy, d.gz};
+    double obj = 0.0, kin = 0.0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double g = k < 3 ? grav[k] * dt * dt : 0.0;
+        const double qo = d.q_old[o + k];
+        const double predicted = qo + dt * d.v[o + k] + g;
+        const double delta = q[k] - predicted, damp = q[k] - qo;
+        const double kk = k < 3 ? kx : kr, c = k < 3 ? cx : cr;
+        obj += 0.5 * kk * delta * delta + 0.5 * c * damp * damp;
+        if (k < 3) kin += 0.5 * m * damp * damp * inv2;
+        if (gradient) {
+            d.grad[o + k] = kk * delta + c * damp;
+            d.diag[36 * size_t(n) + 7 * k] = kk + c;
+        }
+    }
+    d.node_energy[n] = obj;
+    d.node_kinetic[n] = kin;
+}
+
+// Broad + narrow phase of one element: every candidate in traversal order,
+// the first strictly closest triangle kept (cuda_backend.cu:920-926).
+__device__ __forceinline__ uint32_t closest_triangle(const View &d, V xi, V xj, double pad, uint32_t &cand,
+                                                     dm::ClosestPair &pair)
+{
+    uint32_t closest = kNone;
+    cand = 0;
+    pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
+    bvh_query(d, dm::vmin(xi, xj), dm::vmax(xi, xj), pad, [&](uint32_t t) {
+        ++cand;
+        const dm::ClosestPair c = dm::closest_segment_triangle(xi, xj, tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2));
+        if (c.distance < pair.distance) { pair = c; closest = t; }
+    });
+    return closest;
+}
+
+// Contact classification of every element at a caller-provided state
+// (positions of q_probe); used to check the integer contact work.
+__global__ void __launch_bounds__(kBlock) k_contact_query(View d, const double *q)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    uint32_t cand = 0, closest = kNone;
+    uint8_t flags = 0;
+    double gap = 0.0;
+    if (d.has_collider && !d.fixed[i] && d.econtact[e]) {
+        dm::ClosestPair pair;
+        closest = closest_triangle(d, load3(q + 6 * size_t(i)), load3(q + 6 * size_t(j)), d.radius + d.offset + d.dhat, cand, pair);
+        if (closest != kNone) {
+            flags |= kFlagClosest;
+            gap = pair.distance - d.radius - d.offset;
+            if (gap <= d.min_gap) flags |= kFlagInfeasible;
+            else if (gap < d.dhat) flags |= kFlagActive;
+        }
+    }
+    d.c_cand[e] = cand;
+    d.c_tri[e] = closest;
+    d.c_flags[e] = flags;
+    d.c_gap[e] = gap;
+}
+
+// Per element: elastic energy (+ gradient and GN blocks) and barrier contact
+// against the closest BVH candidate (cuda_backend.cu:899-939).
+__global__ void __launch_bounds__(kBlock) k_elem_eval(View d, int gradient)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    const bool fi = d.fixed[i], fj = d.fixed[j];
+    const V xi = load3(d.q + 6 * size_t(i)), xj = load3(d.q + 6 * size_t(j));
+    const M Ri = load9(d.rot + 9 * size_t(i)), Rj = load9(d.rot + 9 * size_t(j));
+    const double L0 = d.L0[e];
+    double eps[6];
+    double *gi = d.as_i_g + 6 * size_t(i), *gj = d.as_j_g + 6 * size_t(j);
+    double *Hii = d.as_i_h + 36 * size_t(i), *Hjj = d.as_j_h + 36 * size_t(j), *Hij = d.upper + 36 * size_t(i);
+    if (gradient) {
+        const M Jli = load9(d.jl + 9 * size_t(i)), Jlj = load9(d.jl + 9 * size_t(j));
+        dm::ElementJacobian J;
+        dm::element_strain(Ri, Rj, xi, xj, L0, load3(d.gamma0 + 3 * size_t(e)), load3(d.kappa0 + 3 * size_t(e)), eps, &J,
+                           &Jli, &Jlj);
+        double a[6], b[6];
+        dm::element_gradient(J, eps, d.w, L0, a, b);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { gi[k] = fi ? 0.0 : a[k]; gj[k] = fj ? 0.0 : b[k]; }
+        double hii[36], hjj[36], hij[36];
+        dm::element_hessian(J, d.w, L0, hii, hjj, hij);
+        for (int k = 0; k < 36; ++k) {
+            Hii[k] = fi ? 0.0 : hii[k];
+            Hjj[k] = fj ? 0.0 : hjj[k];
+            Hij[k] = (fi || fj) ? 0.0 : hij[k];
+        }
+    } else {
+        dm::element_strain(Ri, Rj, xi, xj, L0, load3(d.gamma0 + 3 * size_t(e)), load3(d.kappa0 + 3 * size_t(e)), eps,
+                           nullptr, nullptr, nullptr);
+    }
+    d.e_el[e] = dm::element_energy(eps, d.w, L0);
+
+    uint32_t cand = 0, closest = kNone;
+    uint8_t flags = 0;
+    double gap = 0.0, ce = 0.0;
+    if (d.has_collider && !fi && d.econtact[e]) {
+        dm::ClosestPair pair;
+        closest = closest_triangle(d, xi, xj, d.radius + d.offset + d.dhat, cand, pair);
+        if (closest != kNone) {
+            flags |= kFlagClosest;
+            gap = pair.distance - d.radius - d.offset;
+            if (gap <= d.min_gap) flags |= kFlagInfeasible;
+            else if (gap < d.dhat) {
+                flags |= kFlagActive;
+                const V a = tri_vertex(d, closest, 0), b = tri_vertex(d, closest, 1), c = tri_vertex(d, closest, 2);
+                const V bp = a * pair.bary.x + b * pair.bary.y + c * pair.bary.z;
+                double g0[3], g1[3];
+                const double energy = dm::barrier_energy_gradient(xi, xj, pair.t, bp, d.radius + d.offset, d.dhat, d.kc, g0, g1);
+                if (!isfinite(energy)) flags |= kFlagInfeasible;
+                else {
+                    flags |= kFlagEnergy;
+                    ce = energy;
+                    if (gradient) {
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) { gi[k] += g0[k]; gj[k] += g1[k]; }
+                        const V normal = (xi * (1.0 - pair.t) + xj * pair.t - bp) * (1.0 / fmax(pair.distance, 1e-15));
+                        const double aa = d.dhat - gap;
+                        const double curv = d.kc * (-2.0 * log(gap / d.dhat) + 4.0 * aa / gap + aa * aa / (gap * gap));
+                        const double dg[6] = {normal.x * (1.0 - pair.t), normal.y * (1.0 - pair.t), normal.z * (1.0 - pair.t),
+                                              normal.x * pair.t, normal.y * pair.t, normal.z * pair.t};
+#pragma unroll
+                        for (int r = 0; r < 3; ++r)
+#pragma unroll
+                            for (int c2 = 0; c2 < 3; ++c2) {
+                                Hii[6 * r + c2] += curv * dg[r] * dg[c2];
+                                Hjj[6 * r + c2] += curv * dg[3 + r] * dg[3 + c2];
+                                Hij[6 * r + c2] += curv * dg[r] * dg[3 + c2];
+                            }
+                    }
+                }
+            }
+        }
+    }
+    d.e_co[e] = ce;
+    d.c_cand[e] = cand;
+    d.c_tri[e] = closest;
+    d.c_flags[e] = flags;
+    d.c_gap[e] = gap;
+}
+
+// Node sums in a fixed order: inertia, then the element on the left (this
+// node as its right end), then the element on the right.
+__global__ void __launch_bounds__(kBlock) k_node_sum(View d)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    const size_t o6 = 6 * size_t(n), o36 = 36 * size_t(n);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) d.grad[o6 + k] = (d.grad[o6 + k] + d.as_j_g[o6 + k]) + d.as_i_g[o6 + k];
+    for (int k = 0; k < 36; ++k) d.diag[o36 + k] = (d.diag[o36 + k] + d.as_j_h[o36 + k]) + d.as_i_h[o36 + k];
+}
+
+// Block-level tree sum of one double per thread (blockDim == kBlock).
+__device__ double block_sum(double x, double *sh)
+{
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int s = kBlock / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+__device__ double block_min(double x, double *sh)
+{
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int s = kBlock / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+__device__ double block_max(double x, double *sh)
+{
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int s = kBlock / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+__device__ unsigned long long block_sum_u(unsigned long long x, unsigned long long *sh)
+{
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int s = kBlock / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    const unsigned long long r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ void chunk(uint32_t count, uint32_t &begin, uint32_t &end)
+{
+    const uint64_t b = uint64_t(blockIdx.x) * count / gridDim.x, e = uint64_t(blockIdx.x + 1) * count / gridDim.x;
+    begin = uint32_t(b);
+    end = uint32_t(e);
+}
+
+// First reduction level over nodes and elements of this block's chunk.
+__global__ void __launch_bounds__(kBlock) k_reduce_eval(View d, int gradient)
+{
+    __shared__ double sh[kBlock];
+    __shared__ unsigned long long shu[kBlock];
+    uint32_t nb, ne, eb, ee;
+    chunk(d.N, nb, ne);
+    chunk(d.E, eb, ee);
+    double en = 0.0, ki = 0.0, g2 = 0.0, el = 0.0, co = 0.0, mg = __longlong_as_double(0x7ff0000000000000LL);
+    unsigned long long cand = 0, act = 0;
+    int inf = 0;
+    for (uint32_t n = nb + threadIdx.x; n < ne; n += kBlock) {
+        en += d.node_energy[n];
+        ki += d.node_kinetic[n];
+        if (gradient)
+            for (int k = 0; k < 6; ++k) { const double g = d.grad[6 * size_t(n) + k]; g2 += g * g; }
+    }
+    for (uint32_t e = eb + threadIdx.x; e < ee; e += kBlock) {
+        el += d.e_el[e];
+        co += d.e_co[e];
+        cand += d.c_cand[e];
+        const uint8_t f = d.c_flags[e];
+        if (f & kFlagClosest) mg = fmin(mg, d.c_gap[e]);
+        if (f & kFlagActive) ++act;
+        if (f & kFlagInfeasible) inf = 1;
+    }
+    Partial p;
+    p.node_energy = block_sum(en, sh);
+    p.kinetic = block_sum(ki, sh);
+    p.grad2 = block_sum(g2, sh);
+    p.elastic = block_sum(el, sh);
+    p.contact = block_sum(co, sh);
+    p.min_gap = block_min(mg, sh);
+    p.candidates = block_sum_u(cand, shu);
+    p.active = block_sum_u(act, shu);
+    p.infeasible = int(block_sum_u((unsigned long long)inf, shu) != 0);
+    p.pad = 0;
+    if (threadIdx.x == 0) d.partials[blockIdx.x] = p;
+}
+
+__global__ void __launch_bounds__(kBlock) k_final_eval(View d)
+{
+    __shared__ double sh[kBlock];
+    __shared__ unsigned long long shu[kBlock];
+    double en = 0, ki = 0, g2 = 0, el = 0, co = 0, mg = __longlong_as_double(0x7ff0000000000000LL);
+    unsigned long long cand = 0, act = 0, inf = 0;
+    for (int b = threadIdx.x; b < kPartials; b += kBlock) {
+        const Partial p = d.partials[b];
+        en += p.node_energy; ki += p.kinetic; g2 += p.grad2; el += p.elastic; co += p.contact;
+        mg = fmin(mg, p.min_gap);
+        cand += p.candidates; act += p.active; inf += p.infeasible;
+    }
+    en = block_sum(en, sh); ki = block_sum(ki, sh); g2 = block_sum(g2, sh);
+    el = block_sum(el, sh); co = block_sum(co, sh); mg = block_min(mg, sh);
+    cand = block_sum_u(cand, shu); act = block_sum_u(act, shu); inf = block_sum_u(inf, shu);
+    if (threadIdx.x == 0) {
+        Mailbox *m = d.mail;
+        m->objective = (en + el) + co;
+        m->elastic = el; m->contact = co; m->kinetic = ki; m->minimum_gap = mg; m->grad_norm2 = g2;
+        m->candidates = cand; m->active = act; m->feasible = inf ? 0 : 1;
+    }
+}
+
+// ---- direction ----------------------------------------------------------
+
+// Gauss-Jordan 6x6 inverse with partial pivoting after a relative diagonal
+// shift (cuda_backend.cu:855-864).
+__device__ bool inverse6(double a[36], double inv[36])
+{
+    for (int k = 0; k < 36; ++k) inv[k] = 0.0;
+    for (int k = 0; k < 6; ++k) inv[7 * k] = 1.0;
+    double scale = 0.0;
+    for (int k = 0; k < 6; ++k) scale = fmax(scale, fabs(a[7 * k]));
+    for (int k = 0; k < 6; ++k) a[7 * k] += fmax(1.0e-12 * scale, 1.0e-24);
+    for (int col = 0; col < 6; ++col) {
+        int pivot = col;
+        double best = fabs(a[6 * col + col]);
+        for (int row = col + 1; row < 6; ++row)
+            if (fabs(a[6 * row + col]) > best) { best = fabs(a[6 * row + col]); pivot = row; }
+        if (best < 1.0e-30 || !isfinite(best)) return false;
+        if (pivot != col)
+            for (int k = 0; k < 6; ++k) {
+                double t = a[6 * col + k]; a[6 * col + k] = a[6 * pivot + k]; a[6 * pivot + k] = t;
+                t = inv[6 * col + k]; inv[6 * col + k] = inv[6 * pivot + k]; inv[6 * pivot + k] = t;
+            }
+        const double ip = 1.0 / a[6 * col + col];
+        for (int k = 0; k < 6; ++k) { a[6 * col + k] *= ip; inv[6 * col + k] *= ip; }
+        for (int row = 0; row < 6; ++row)
+            if (row != col) {
+                const double f = a[6 * row + col];
+                for (int k = 0; k < 6; ++k) { a[6 * row + k] -= f * a[6 * col + k]; inv[6 * row + k] -= f * inv[6 * col + k]; }
+            }
+    }
+    return true;
+}
+
+// Block-tridiagonal Thomas solve per strand (cuda_backend.cu:866-881),
+// row-parallel: a group of 6 lanes owns one strand and lane r holds row r of
+// every 6x6 block (B, its Gauss-Jordan inverse, C = B^-1 U), so a warp
+// solves 5 strands at once and the 6x6 algebra runs on 30 lanes with
+// shuffles for the pivot search, row swaps and row broadcasts.  Strands are
+// taken in length-sorted order so the 5 strands of a warp have similar
+// lengths.  The inverse is the reference's Gauss-Jordan elimination with
+// partial pivoting (first largest pivot) after the relative diagonal shift
+// max(1e-12 max|a_ii|, 1e-24) (cuda_backend.cu:855-864).
+constexpr int kSolveGroup = 6, kSolveGroupsPerWarp = 5;
+
+__global__ void __launch_bounds__(128) k_block_solve(View d)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int grp = lane / kSolveGroup, r = lane % kSolveGroup, base = grp * kSolveGroup;
+    const uint32_t k = warp * kSolveGroupsPerWarp + uint32_t(grp);
+    const bool member = grp < kSolveGroupsPerWarp && k < d.S;
+    uint32_t begin = 0, len = 0;
+    if (member) {
+        const uint32_t s = d.sorder[k];
+        begin = d.sfirst[s] + d.sfixed[s];
+        const uint32_t end = d.sfirst[s] + d.scount[s];
+        len = end > begin ? end - begin : 0;
+    }
+    uint32_t maxlen = len;
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(FULL, maxlen, o));
+    double Crow[6] = {0, 0, 0, 0, 0, 0}, dprev = 0.0;
+    bool failed = false;
+    for (uint32_t t = 0; t < maxlen; ++t) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        double a[6], inv[6], rhs = 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { a[c] = on ? d.diag[36 * n + 6 * r + c] : 0.0; inv[c] = (c == r) ? 1.0 : 0.0; }
+        if (on) rhs = -d.grad[6 * n + r];
+        if (t > 0) {
+            // B -= U_{n-1}^T C_{n-1}, rhs -= U_{n-1}^T d'_{n-1}
+            double ucol[6];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) ucol[q] = on ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
+            double sum[6] = {0, 0, 0, 0, 0, 0}, sr = 0.0;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) sum[c] += ucol[q] * __shfl_sync(FULL, Crow[c], base + q);
+                sr += ucol[q] * __shfl_sync(FULL, dprev, base + q);
+            }
+#pragma unroll
+            for (int c = 0; c < 6; ++c) a[c] -= sum[c];
+            rhs -= sr;
+        }
+        // Relative diagonal shift.
+        double diag_r = 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) if (c == r) diag_r = a[c];
+        double scale = 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) scale = fmax(scale, fabs(__shfl_sync(FULL, diag_r, base + q)));
+        const double shift = fmax(1.0e-12 * scale, 1.0e-24);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) if (c == r) a[c] += shift;
+        // Gauss-Jordan with partial pivoting.
+        bool ok = true;
+#pragma unroll
+        for (int col = 0; col < 6; ++col) {
+            double mine = 0.0;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) if (c == col) mine = a[c];
+            int pivot = col;
+            double best = fabs(__shfl_sync(FULL, mine, base + col));
+#pragma unroll
+            for (int row = col + 1; row < 6; ++row) {
+                const double vrow = fabs(__shfl_sync(FULL, mine, base + row));
+                if (vrow > best) { best = vrow; pivot = row; }
+            }
+            if (best < 1.0e-30 || !isfinite(best)) ok = false;
+            // Swap rows col and pivot.
+            const int partner = r == col ? pivot : (r == pivot ? col : r);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                a[c] = __shfl_sync(FULL, a[c], base + partner);
+                inv[c] = __shfl_sync(FULL, inv[c], base + partner);
+            }
+            // Normalise the pivot row and eliminate the column elsewhere.
+            double pv = 0.0;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) if (c == col) pv = a[c];
+            const double ip = 1.0 / __shfl_sync(FULL, pv, base + col);
+            double prow[6], pinv[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                prow[c] = __shfl_sync(FULL, a[c], base + col) * ip;
+                pinv[c] = __shfl_sync(FULL, inv[c], base + col) * ip;
+            }
+            if (r == col) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) { a[c] = prow[c]; inv[c] = pinv[c]; }
+            } else {
+                double f = 0.0;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) if (c == col) f = a[c];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) { a[c] -= f * prow[c]; inv[c] -= f * pinv[c]; }
+            }
+        }
+        if (on && !ok) {
+            failed = true;
+            if (r == 0) atomicExch(&d.sc->solve_failed, 1);
+        }
+        // C_n = B^-1 U_n (zero at the strand tip), d'_n = B^-1 rhs.
+        const bool last = t + 1 >= len;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            double sum = 0.0;
+            if (on && !last)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) sum += inv[q] * d.upper[36 * n + 6 * q + c];
+            Crow[c] = sum;
+        }
+        double dn = 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) dn += inv[q] * __shfl_sync(FULL, rhs, base + q);
+        dprev = dn;
+        if (on && !failed) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) d.cprime[36 * n + 6 * r + c] = Crow[c];
+            d.dprime[6 * n + r] = dn;
+        }
+    }
+    // Back substitution d_n = d'_n - C_n d_{n+1}.
+    double next = 0.0;
+    for (uint32_t t = maxlen; t-- > 0;) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        double value = on ? d.dprime[6 * n + r] : 0.0;
+        const bool coupled = on && t + 1 < len;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const double dq = __shfl_sync(FULL, next, base + q);  // every lane, every time: no divergent shuffles
+            if (coupled) value -= d.cprime[36 * n + 6 * r + q] * dq;
+        }
+        if (on) d.dir[6 * n + r] = value;
+        next = on ? value : 0.0;
+    }
+}
+
+// Preconditioned steepest descent d = -P g, zero at fixed nodes
+// (cuda_backend.cu:632-638).
+__global__ void __launch_bounds__(kBlock) k_steepest(View d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * d.N) return;
+    d.dir[i] = d.fixed[i / 6] ? 0.0 : -d.grad[i] * d.precond[i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_scale(View d, double s)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * d.N) d.dir[i] *= s;
+}
+
+// g.d, |d|^2 and the largest free-node translation of d.
+__global__ void __launch_bounds__(kBlock) k_reduce_dir(View d)
+{
+    __shared__ double sh[kBlock];
+    uint32_t nb, ne;
+    chunk(d.N, nb, ne);
+    double gd = 0.0, dd = 0.0, mx = 0.0;
+    for (uint32_t n = nb + threadIdx.x; n < ne; n += kBlock) {
+        for (int k = 0; k < 6; ++k) {
+            const double x = d.dir[6 * size_t(n) + k];
+            gd += d.grad[6 * size_t(n) + k] * x;
+            dd += x * x;
+        }
+        if (!d.fixed[n]) mx = fmax(mx, dm::norm(load3(d.dir + 6 * size_t(n))));
+    }
+    DirPartial p;
+    p.slope = block_sum(gd, sh);
+    p.dnorm2 = block_sum(dd, sh);
+    p.max_translation = block_max(mx, sh);
+    if (threadIdx.x == 0) d.dpartials[blockIdx.x] = p;
+}
+
+__global__ void __launch_bounds__(kBlock) k_final_dir(View d)
+{
+    __shared__ double sh[kBlock];
+    double gd = 0, dd = 0, mx = 0;
+    for (int b = threadIdx.x; b < kPartials; b += kBlock) {
+        const DirPartial p = d.dpartials[b];
+        gd += p.slope; dd += p.dnorm2; mx = fmax(mx, p.max_translation);
+    }
+    gd = block_sum(gd, sh); dd = block_sum(dd, sh); mx = block_max(mx, sh);
+    if (threadIdx.x == 0) {
+        d.mail->slope = gd; d.mail->dir_norm2 = dd; d.mail->max_translation = mx;
+        d.mail->ccd_bits = d.sc->ccd_bits;
+        d.mail->solve_failed = d.sc->solve_failed;
+        d.sc->ccd_bits = 0x3ff0000000000000ULL;  // 1.0
+        d.sc->solve_failed = 0;
+    }
+}
+
+// Line-search CCD bound (cuda_backend.cu:989-1000); the minimum over all
+// elements and candidates is taken with an unsigned atomicMin on the bit
+// pattern of the non-negative step.
+__global__ void __launch_bounds__(kBlock) k_ccd(View d)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    if (d.fixed[i] || !d.econtact[e]) return;
+    const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
+    const V d0 = load3(d.dir + 6 * size_t(i)), d1 = load3(d.dir + 6 * size_t(j));
+    const V lo = dm::vmin(dm::vmin(p0, p1), dm::vmin(p0 + d0, p1 + d1));
+    const V hi = dm::vmax(dm::vmax(p0, p1), dm::vmax(p0 + d0, p1 + d1));
+    const double target = d.radius + d.offset + d.min_gap;
+    double local = 1.0;
+    bvh_query(d, lo, hi, target, [&](uint32_t t) {
+        const double speed = fmax(dm::gnorm(d0), dm::gnorm(d1));
+        if (speed < 1e-30) return;
+        const V a = tri_vertex(d, t, 0), b = tri_vertex(d, t, 1), c = tri_vertex(d, t, 2);
+        double alpha = 0.0;
+        for (int k = 0; k < 80; ++k) {
+            const double dist = dm::closest_segment_triangle(dm::gadd(p0, dm::gmul(d0, alpha)), dm::gadd(p1, dm::gmul(d1, alpha)), a, b, c).distance;
+            const double clear = dist - target;
+            if (clear <= 0) { local = fmin(local, fmax(0.0, alpha * 0.9)); return; }
+            const double advance = 0.8 * clear / speed;
+            if (alpha + advance >= 1) return;
+            if (advance < 1e-12) { local = fmin(local, alpha); return; }
+            alpha += advance;
+        }
+        local = fmin(local, alpha);
+    });
+    if (local < 1.0) atomicMin(&d.sc->ccd_bits, (unsigned long long)__double_as_longlong(local));
+}
+
+// ---- end of substep -------------------------------------------------------
+
+__global__ void __launch_bounds__(kBlock) k_update_velocity(View d, double inv_dt)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N || d.fixed[n]) return;
+    for (int k = 0; k < 6; ++k) d.v[6 * size_t(n) + k] = (d.q[6 * size_t(n) + k] - d.q_old[6 * size_t(n) + k]) * inv_dt;
+}
+
+// Coulomb friction impulse (cuda_backend.cu:941-964); each element writes
+// its velocity change into its left/right node slots.
+__global__ void __launch_bounds__(kBlock) k_friction(View d, double dt)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    double di[3] = {0, 0, 0}, dj[3] = {0, 0, 0};
+    const bool fi = d.fixed[i], fj = d.fixed[j];
+    if (d.econtact[e] && !(fi && fj)) {
+        const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
+        uint32_t cand = 0;
+        dm::ClosestPair pair;
+        const uint32_t closest = closest_triangle(d, p0, p1, d.radius + d.offset + d.dhat, cand, pair);
+        const double gap = pair.distance - d.radius - d.offset;
+        if (closest != kNone && gap > 0.0 && gap < d.dhat) {
+            const double w0 = 1.0 - pair.t, w1 = pair.t;
+            const V hair = p0 * w0 + p1 * w1;
+            const V body = tri_vertex(d, closest, 0) * pair.bary.x + tri_vertex(d, closest, 1) * pair.bary.y +
+                           tri_vertex(d, closest, 2) * pair.bary.z;
+            const V ob = load3(d.col_old + 3 * size_t(d.tri[3 * closest])) * pair.bary.x +
+                         load3(d.col_old + 3 * size_t(d.tri[3 * closest + 1])) * pair.bary.y +
+                         load3(d.col_old + 3 * size_t(d.tri[3 * closest + 2])) * pair.bary.z;
+            const V normal = (hair - body) * (1.0 / fmax(pair.distance, 1.0e-15));
+            const V v0 = load3(d.v + 6 * size_t(i)), v1 = load3(d.v + 6 * size_t(j));
+            const V rel = v0 * w0 + v1 * w1 - (body - ob) * (1.0 / dt);
+            const V tangent = rel - normal * dm::dot(normal, rel);
+            const double ts = dm::norm(tangent);
+            double im = 0.0;
+            if (!fi) im += w0 * w0 / fmax(d.mass[i], 1.0e-30);
+            if (!fj) im += w1 * w1 / fmax(d.mass[j], 1.0e-30);
+            if (!(ts < 1.0e-15) && im > 0.0) {
+                const double aa = d.dhat - gap, lg = log(gap / d.dhat);
+                const double fn = d.kc * (aa * aa / gap - 2.0 * aa * lg), required = ts / im;
+                const double mag = fmin(required, d.friction * fn * dt), smooth = d.smoothing / dt;
+                const V imp = tangent * (-mag / fmax(sqrt(ts * ts + smooth * smooth), 1.0e-30));
+                if (!fi) { const double s = w0 / fmax(d.mass[i], 1.0e-30); di[0] = imp.x * s; di[1] = imp.y * s; di[2] = imp.z * s; }
+                if (!fj) { const double s = w1 / fmax(d.mass[j], 1.0e-30); dj[0] = imp.x * s; dj[1] = imp.y * s; dj[2] = imp.z * s; }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { d.as_i_f[3 * size_t(i) + k] = di[k]; d.as_j_f[3 * size_t(j) + k] = dj[k]; }
+}
+
+__global__ void __launch_bounds__(kBlock) k_friction_apply(View d)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d.v[6 * size_t(n) + k] += d.as_j_f[3 * size_t(n) + k] + d.as_i_f[3 * size_t(n) + k];
+}
+
+__global__ void k_init_scalars(View d)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    d.sc->ccd_bits = 0x3ff0000000000000ULL;
+    d.sc->sweep_fail = kNone;
+    d.sc->solve_failed = 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t n = map ? map[i] : i;
+    out[3 * size_t(i)] = q[6 * size_t(n)];
+    out[3 * size_t(i) + 1] = q[6 * size_t(n) + 1];
+    out[3 * size_t(i) + 2] = q[6 * size_t(n) + 2];
+}
+
+// ---- device memory --------------------------------------------------------
+
+struct Arena {
+    char *base = nullptr;
+    size_t size = 0, used = 0;
+    template<class T> T *take(size_t count)
+    {
+        const size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+        T *p = reinterpret_cast<T *>(base + used);
+        used += bytes;
+        return p;
+    }
+};
+
+template<class T> size_t padded(size_t count) { return (count * sizeof(T) + 255) & ~size_t(255); }
+
+}  // namespace
+
+struct Engine::Impl {
+    View v{};
+    Arena arena;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    Mailbox *mail_host = nullptr;
+    SweepRecord *sweep_host = nullptr;
+    // Host copies needed by the control flow.
+    std::vector<uint32_t> mapping;
+    uint32_t original_count = 0;
+    double *mapping_gather_out = nullptr;
+    uint32_t *mapping_dev = nullptr;
+    double *q_snap = nullptr, *v_snap = nullptr;
+    double *root_cur_x = nullptr, *root_cur_r = nullptr, *root_pend_x = nullptr, *root_pend_r = nullptr;
+    double *col_frame_start = nullptr, *col_pending = nullptr;
+    double *anim_root_x = nullptr, *anim_root_r = nullptr, *anim_col = nullptr;
+    size_t anim_bytes = 0;
+    double *col_a_copy = nullptr;  // frame-start copy used while stepping
+    std::vector<uint8_t> fixed_host;
+    uint64_t resident = 0;
+
+    // Per-kernel device-time accounting (CUDA events on this stream).
+    struct KernelStat { const char *name; uint64_t launches; double ms; };
+    bool profiling = false;
+    uint64_t launches = 0;
+    std::vector<KernelStat> kstats;
+    std::vector<std::pair<size_t, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::vector<cudaEvent_t> pool;
+
+    cudaEvent_t take_event()
+    {
+        if (pool.empty()) {
+            cudaEvent_t e;
+            KHS_CUDA(cudaEventCreate(&e));
+            return e;
+        }
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    size_t stat_index(const char *name)
+    {
+        for (size_t k = 0; k < kstats.size(); ++k)
+            if (kstats[k].name == name) return k;
+        kstats.push_back({name, 0, 0.0});
+        return kstats.size() - 1;
+    }
+    template<class K, class... A> void launch(const char *name, K kernel, unsigned grid, unsigned block, A... args)
+    {
+        ++launches;
+        if (!profiling) {
+            kernel<<<grid, block, 0, stream>>>(args...);
+            return;
+        }
+        cudaEvent_t a = take_event(), b = take_event();
+        KHS_CUDA(cudaEventRecord(a, stream));
+        kernel<<<grid, block, 0, stream>>>(args...);
+        KHS_CUDA(cudaEventRecord(b, stream));
+        pending.push_back({stat_index(name), {a, b}});
+    }
+    void resolve()
+    {
+        for (auto &p : pending) {
+            float ms = 0.0f;
+            KHS_CUDA(cudaEventElapsedTime(&ms, p.second.first, p.second.second));
+            kstats[p.first].launches += 1;
+            kstats[p.first].ms += ms;
+            pool.push_back(p.second.first);
+            pool.push_back(p.second.second);
+        }
+        pending.clear();
+    }
+
+    ~Impl()
+    {
+        for (auto &p : pending) { pool.push_back(p.second.first); pool.push_back(p.second.second); }
+        for (cudaEvent_t e : pool) cudaEventDestroy(e);
+        if (arena.base) cudaFree(arena.base);
+        if (anim_root_x) cudaFree(anim_root_x);
+        if (mail_host) cudaFreeHost(mail_host);
+        if (sweep_host) cudaFreeHost(sweep_host);
+        if (ev_begin) cudaEventDestroy(ev_begin);
+        if (ev_end) cudaEventDestroy(ev_end);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    void sync()
+    {
+        KHS_CUDA(cudaStreamSynchronize(stream));
+        if (!pending.empty()) resolve();
+    }
+    void check() { KHS_CUDA(cudaGetLastError()); }
+};
+
+Engine::Engine() : d_(new Impl) {}
+Engine::~Engine() = default;
+
+void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHairMaterial &material,
+                        const std::vector<Vec> &root_pos, const std::vector<Vec> &root_rot)
+{
+    Impl &I = *d_;
+    KHS_CUDA(cudaSetDevice(0));
+    KHS_CUDA(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
+    KHS_CUDA(cudaEventCreate(&I.ev_begin));
+    KHS_CUDA(cudaEventCreate(&I.ev_end));
+    KHS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&I.mail_host), sizeof(Mailbox), cudaHostAllocMapped));
+    KHS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&I.sweep_host), sizeof(SweepRecord), cudaHostAllocMapped));
+    std::memset(I.mail_host, 0, sizeof(Mailbox));
+    std::memset(I.sweep_host, 0, sizeof(SweepRecord));
+    desc_ = desc;
+    material_ = material;
+    const size_t N = m.nodes(), E = m.elements(), S = m.strands(), Vn = m.collider.size(), T = m.tri.size() / 3,
+                 B = m.bvh.size(), L = m.bvh.leaves.size(), O = m.mapping.size();
+    // Arena sizing.
+    size_t bytes = 0;
+    bytes += 12 * padded<double>(6 * N);     // q q_old v q_base grad dir precond dprime as_i_g as_j_g q_snap v_snap
+    bytes += 5 * padded<double>(36 * N);     // diag upper cprime as_i_h as_j_h
+    bytes += 2 * padded<double>(9 * N) + padded<double>(9 * N);  // rot jl ref
+    bytes += 4 * padded<double>(N);          // node_energy kinetic mass rmass
+    bytes += 2 * padded<double>(3 * N);      // as_i_f as_j_f
+    bytes += padded<uint8_t>(N) + 2 * padded<int32_t>(N);
+    bytes += 4 * padded<double>(3 * N);      // root cur/pending x r
+    bytes += 3 * padded<uint32_t>(E) + padded<uint8_t>(E) + padded<double>(E) + 2 * padded<double>(3 * E);
+    bytes += 3 * padded<double>(E) + 2 * padded<uint32_t>(E) + padded<uint8_t>(E);
+    bytes += 4 * padded<uint32_t>(S);
+    bytes += padded<uint32_t>(3 * T) + 5 * padded<double>(3 * Vn);
+    bytes += 2 * padded<double>(3 * B) + 4 * padded<uint32_t>(B) + padded<int32_t>(B) + 2 * padded<uint32_t>(B) +
+             padded<uint32_t>(L) + padded<uint32_t>(T);
+    bytes += padded<Partial>(kPartials) + padded<DirPartial>(kPartials) + padded<Scalars>(1);
+    bytes += padded<uint32_t>(O) + padded<double>(3 * std::max(N, O));
+    KHS_CUDA(cudaMalloc(reinterpret_cast<void **>(&I.arena.base), bytes));
+    KHS_CUDA(cudaMemsetAsync(I.arena.base, 0, bytes, I.stream));
+    I.arena.size = bytes;
+    I.resident = bytes;
+    Arena &a = I.arena;
+    View &v = I.v;
+    v.N = uint32_t(N); v.E = uint32_t(E); v.S = uint32_t(S); v.V = uint32_t(Vn); v.T = uint32_t(T); v.B = uint32_t(B);
+    v.L = uint32_t(L);
+    v.q = a.take<double>(6 * N); v.q_old = a.take<double>(6 * N); v.v = a.take<double>(6 * N);
+    v.q_base = a.take<double>(6 * N); v.grad = a.take<double>(6 * N); v.dir = a.take<double>(6 * N);
+    v.precond = a.take<double>(6 * N); v.dprime = a.take<double>(6 * N);
+    v.as_i_g = a.take<double>(6 * N); v.as_j_g = a.take<double>(6 * N);
+    I.q_snap = a.take<double>(6 * N); I.v_snap = a.take<double>(6 * N);
+    v.diag = a.take<double>(36 * N); v.upper = a.take<double>(36 * N); v.cprime = a.take<double>(36 * N);
+    v.as_i_h = a.take<double>(36 * N); v.as_j_h = a.take<double>(36 * N);
+    v.rot = a.take<double>(9 * N); v.jl = a.take<double>(9 * N);
+    double *ref = a.take<double>(9 * N);
+    v.node_energy = a.take<double>(N); v.node_kinetic = a.take<double>(N);
+    double *mass = a.take<double>(N), *rmass = a.take<double>(N);
+    v.as_i_f = a.take<double>(3 * N); v.as_j_f = a.take<double>(3 * N);
+    uint8_t *fixed = a.take<uint8_t>(N);
+    int32_t *eleft = a.take<int32_t>(N), *eright = a.take<int32_t>(N);
+    I.root_cur_x = a.take<double>(3 * N); I.root_cur_r = a.take<double>(3 * N);
+    I.root_pend_x = a.take<double>(3 * N); I.root_pend_r = a.take<double>(3 * N);
+    uint32_t *ei = a.take<uint32_t>(E), *ej = a.take<uint32_t>(E), *es = a.take<uint32_t>(E);
+    uint8_t *ec = a.take<uint8_t>(E);
+    double *L0 = a.take<double>(E), *g0 = a.take<double>(3 * E), *k0 = a.take<double>(3 * E);
+    v.e_el = a.take<double>(E); v.e_co = a.take<double>(E); v.c_gap = a.take<double>(E);
+    v.c_cand = a.take<uint32_t>(E); v.c_tri = a.take<uint32_t>(E); v.c_flags = a.take<uint8_t>(E);
+    uint32_t *sf = a.take<uint32_t>(S), *sc = a.take<uint32_t>(S), *sx = a.take<uint32_t>(S), *so = a.take<uint32_t>(S);
+    uint32_t *tri = a.take<uint32_t>(3 * T);
+    v.col_cur = a.take<double>(3 * Vn); v.col_old = a.take<double>(3 * Vn);
+    I.col_frame_start = a.take<double>(3 * Vn); I.col_pending = a.take<double>(3 * Vn); I.col_a_copy = a.take<double>(3 * Vn);
+    v.blo = a.take<double>(3 * B); v.bhi = a.take<double>(3 * B);
+    uint32_t *besc = a.take<uint32_t>(B), *bfirst = a.take<uint32_t>(B), *bcount = a.take<uint32_t>(B);
+    v.brefit = a.take<uint32_t>(B);
+    int32_t *bparent = a.take<int32_t>(B);
+    uint32_t *bleft = a.take<uint32_t>(B), *bright = a.take<uint32_t>(B), *bleaves = a.take<uint32_t>(L);
+    uint32_t *border = a.take<uint32_t>(T);
+    v.partials = a.take<Partial>(kPartials);
+    v.dpartials = a.take<DirPartial>(kPartials);
+    v.sc = a.take<Scalars>(1);
+    I.mapping_dev = a.take<uint32_t>(O);
+    I.mapping_gather_out = a.take<double>(3 * std::max(N, O));
+    if (a.used > a.size) throw std::runtime_error("device arena overflow");
+
+    // Host staging.
+    auto up = [&](void *dst, const void *src, size_t bytes2) {
+        if (bytes2) KHS_CUDA(cudaMemcpyAsync(dst, src, bytes2, cudaMemcpyHostToDevice, I.stream));
+    };
+    std::vector<double> hq(6 * N, 0.0), href(9 * N);
+    std::vector<int32_t> hl(N, -1), hr(N, -1);
+    for (size_t n = 0; n < N; ++n) {
+        hq[6 * n] = m.x[n].x; hq[6 * n + 1] = m.x[n].y; hq[6 * n + 2] = m.x[n].z;
+        std::memcpy(&href[9 * n], m.frame[n].m, 9 * sizeof(double));
+    }
+    for (size_t e = 0; e < E; ++e) { hr[m.elem_i[e]] = int32_t(e); hl[m.elem_j[e]] = int32_t(e); }
+    std::vector<double> hg0(3 * E), hk0(3 * E);
+    for (size_t e = 0; e < E; ++e) {
+        hg0[3 * e] = m.rest_shear[e].x; hg0[3 * e + 1] = m.rest_shear[e].y; hg0[3 * e + 2] = m.rest_shear[e].z;
+        hk0[3 * e] = m.rest_curvature[e].x; hk0[3 * e + 1] = m.rest_curvature[e].y; hk0[3 * e + 2] = m.rest_curvature[e].z;
+    }
+    std::vector<uint32_t> order(S);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) {
+        return m.strand_count[l] - m.strand_fixed[l] > m.strand_count[r] - m.strand_fixed[r];
+    });
+    std::vector<double> hcol(3 * Vn);
+    for (size_t k = 0; k < Vn; ++k) { hcol[3 * k] = m.collider[k].x; hcol[3 * k + 1] = m.collider[k].y; hcol[3 * k + 2] = m.collider[k].z; }
+    std::vector<double> hrx(3 * N), hrr(3 * N);
+    for (size_t n = 0; n < N; ++n) {
+        hrx[3 * n] = root_pos[n].x; hrx[3 * n + 1] = root_pos[n].y; hrx[3 * n + 2] = root_pos[n].z;
+        hrr[3 * n] = root_rot[n].x; hrr[3 * n + 1] = root_rot[n].y; hrr[3 * n + 2] = root_rot[n].z;
+    }
+    up(v.q, hq.data(), 6 * N * 8); up(v.q_old, hq.data(), 6 * N * 8); up(I.q_snap, hq.data(), 6 * N * 8);
+    up(v.q_base, hq.data(), 6 * N * 8);
+    up(ref, href.data(), 9 * N * 8);
+    up(mass, m.mass.data(), N * 8); up(rmass, m.rotational_mass.data(), N * 8);
+    up(fixed, m.fixed.data(), N);
+    up(eleft, hl.data(), N * 4); up(eright, hr.data(), N * 4);
+    up(I.root_cur_x, hrx.data(), 3 * N * 8); up(I.root_cur_r, hrr.data(), 3 * N * 8);
+    up(I.root_pend_x, hrx.data(), 3 * N * 8); up(I.root_pend_r, hrr.data(), 3 * N * 8);
+    up(ei, m.elem_i.data(), E * 4); up(ej, m.elem_j.data(), E * 4); up(es, m.elem_strand.data(), E * 4);
+    up(ec, m.elem_contact.data(), E);
+    up(L0, m.rest_length.data(), E * 8); up(g0, hg0.data(), 3 * E * 8); up(k0, hk0.data(), 3 * E * 8);
+    up(sf, m.strand_first.data(), S * 4); up(sc, m.strand_count.data(), S * 4); up(sx, m.strand_fixed.data(), S * 4);
+    up(so, order.data(), S * 4);
+    up(tri, m.tri.data(), 3 * T * 4);
+    up(v.col_cur, hcol.data(), 3 * Vn * 8); up(v.col_old, hcol.data(), 3 * Vn * 8);
+    up(I.col_frame_start, hcol.data(), 3 * Vn * 8); up(I.col_pending, hcol.data(), 3 * Vn * 8);
+    if (B) {
+        up(v.blo, m.bvh.lower.data(), 3 * B * 8); up(v.bhi, m.bvh.upper.data(), 3 * B * 8);
+        up(besc, m.bvh.escape.data(), B * 4); up(bfirst, m.bvh.first.data(), B * 4); up(bcount, m.bvh.count.data(), B * 4);
+        up(bparent, m.bvh.parent.data(), B * 4); up(bleft, m.bvh.left_child.data(), B * 4);
+        up(bright, m.bvh.right_child.data(), B * 4); up(bleaves, m.bvh.leaves.data(), L * 4);
+        up(border, m.bvh.order.data(), T * 4);
+    }
+    up(I.mapping_dev, m.mapping.data(), O * 4);
+    v.ref = ref; v.mass = mass; v.rmass = rmass; v.fixed = fixed; v.elem_left = eleft; v.elem_right = eright;
+    v.ei = ei; v.ej = ej; v.estrand = es; v.econtact = ec; v.L0 = L0; v.gamma0 = g0; v.kappa0 = k0;
+    v.sfirst = sf; v.scount = sc; v.sfixed = sx; v.sorder = so; v.tri = tri;
+    v.besc = besc; v.bfirst = bfirst; v.bcount = bcount; v.border = border; v.bleaves = bleaves; v.bparent = bparent;
+    v.bleft = bleft; v.bright = bright;
+    KHS_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&v.mail), I.mail_host, 0));
+    KHS_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&v.sweep), I.sweep_host, 0));
+    v.has_collider = T > 0 ? 1 : 0;
+    I.launch("k_init_scalars", k_init_scalars, 1, 1, v);
+    KHS_CUDA(cudaGetLastError());
+    I.original_count = uint32_t(O);
+    I.fixed_host = m.fixed;
+    max_rest_length_ = 0.0;
+    for (double L : m.rest_length) max_rest_length_ = std::fmax(max_rest_length_, L);
+    update_runtime(desc, material, m.mass, m.rotational_mass);
+    I.sync();
+    clear_failure();
+    step_stats_ = {};
+    step_stats_.struct_size = sizeof(step_stats_);
+    gpu_stats_ = {};
+    gpu_stats_.struct_size = sizeof(gpu_stats_);
+    gpu_stats_.resident_bytes = I.resident;
+    initialized_ = true;
+}
+
+void Engine::update_runtime(const KhsSolverDesc &desc, const KhsHairMaterial &material, const std::vector<double> &mass,
+                            const std::vector<double> &rotational_mass)
+{
+    Impl &I = *d_;
+    desc_ = desc;
+    material_ = material;
+    View &v = I.v;
+    if (initialized_ || !mass.empty()) {
+        KHS_CUDA(cudaMemcpyAsync(const_cast<double *>(v.mass), mass.data(), mass.size() * 8, cudaMemcpyHostToDevice, I.stream));
+        KHS_CUDA(cudaMemcpyAsync(const_cast<double *>(v.rmass), rotational_mass.data(), rotational_mass.size() * 8,
+                                 cudaMemcpyHostToDevice, I.stream));
+        I.sync();
+    }
+    v.radius = material.radius; v.offset = material.collider_offset; v.dhat = material.barrier_distance;
+    v.kc = material.contact_stiffness; v.friction = material.friction; v.smoothing = material.friction_smoothing;
+    v.damping = material.mass_damping; v.min_gap = desc.minimum_gap;
+    v.gx = desc.gravity.x; v.gy = desc.gravity.y; v.gz = desc.gravity.z;
+    v.young = material.young_modulus; v.poisson = material.poisson_ratio; v.shear_corr = material.shear_correction;
+    v.w = dm::strain_weights(material.radius, material.young_modulus, material.poisson_ratio, material.shear_correction);
+    trust_radius_ = std::fmax(0.25 * max_rest_length_, 8.0 * (material.radius + material.collider_offset + material.barrier_distance));
+}
+
+void Engine::set_pending_roots(const std::vector<Vec> &pos, const std::vector<Vec> &rot)
+{
+    Impl &I = *d_;
+    const size_t N = I.v.N;
+    std::vector<double> x(3 * N), r(3 * N);
+    for (size_t n = 0; n < N; ++n) {
+        x[3 * n] = pos[n].x; x[3 * n + 1] = pos[n].y; x[3 * n + 2] = pos[n].z;
+        r[3 * n] = rot[n].x; r[3 * n + 1] = rot[n].y; r[3 * n + 2] = rot[n].z;
+    }
+    KHS_CUDA(cudaMemcpyAsync(I.root_pend_x, x.data(), x.size() * 8, cudaMemcpyHostToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.root_pend_r, r.data(), r.size() * 8, cudaMemcpyHostToDevice, I.stream));
+    I.sync();
+}
+
+void Engine::set_pending_collider(const std::vector<Vec> &vertices)
+{
+    Impl &I = *d_;
+    KHS_CUDA(cudaMemcpyAsync(I.col_pending, vertices.data(), vertices.size() * sizeof(Vec), cudaMemcpyHostToDevice, I.stream));
+    I.sync();
+}
+
+KhsResult Engine::allocate_animation(uint32_t frames)
+{
+    Impl &I = *d_;
+    if (!initialized_ || frames < 1) return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid animation frame count");
+    if (I.anim_root_x) { cudaFree(I.anim_root_x); I.anim_root_x = nullptr; I.resident -= I.anim_bytes; }
+    const size_t N = I.v.N, Vn = I.v.V;
+    const size_t root_bytes = size_t(frames) * 3 * N * 8, col_bytes = size_t(frames) * 3 * Vn * 8;
+    const size_t total = 2 * padded<char>(root_bytes) + padded<char>(col_bytes);
+    char *base = nullptr;
+    if (cudaMalloc(reinterpret_cast<void **>(&base), total) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(KHS_ERROR_OUT_OF_MEMORY, "cannot allocate device animation storage");
+    }
+    I.anim_root_x = reinterpret_cast<double *>(base);
+    I.anim_root_r = reinterpret_cast<double *>(base + padded<char>(root_bytes));
+    I.anim_col = reinterpret_cast<double *>(base + 2 * padded<char>(root_bytes));
+    I.anim_bytes = total;
+    I.resident += total;
+    animation_frames_ = frames;
+    animation_ready_ = false;
+    root_frame_set_.assign(frames, false);
+    collider_frame_set_.assign(frames, Vn == 0);
+    gpu_stats_.animation_frame_count = frames;
+    gpu_stats_.resident_bytes = I.resident;
+    return KHS_OK;
+}
+
+KhsResult Engine::set_root_animation_frame(uint32_t frame, const std::vector<Vec> &pos, const std::vector<Vec> &rot)
+{
+    Impl &I = *d_;
+    const size_t N = I.v.N;
+    if (frame >= animation_frames_ || pos.size() != N || rot.size() != N)
+        return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid root animation frame");
+    KHS_CUDA(cudaMemcpyAsync(I.anim_root_x + size_t(frame) * 3 * N, pos.data(), 3 * N * 8, cudaMemcpyHostToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.anim_root_r + size_t(frame) * 3 * N, rot.data(), 3 * N * 8, cudaMemcpyHostToDevice, I.stream));
+    I.sync();
+    root_frame_set_[frame] = true;
+    return KHS_OK;
+}
+
+KhsResult Engine::set_collider_animation_frame(uint32_t frame, const KhsVec3 *vertices, uint32_t count)
+{
+    Impl &I = *d_;
+    if (frame >= animation_frames_ || count != I.v.V) return fail(KHS_ERROR_INVALID_COLLIDER, "invalid collider animation frame");
+    if (count) {
+        KHS_CUDA(cudaMemcpyAsync(I.anim_col + size_t(frame) * 3 * I.v.V, vertices, size_t(count) * 24, cudaMemcpyHostToDevice, I.stream));
+        I.sync();
+    }
+    collider_frame_set_[frame] = true;
+    return KHS_OK;
+}
+
+KhsResult Engine::finalize_animation()
+{
+    if (animation_frames_ < 1 || std::find(root_frame_set_.begin(), root_frame_set_.end(), false) != root_frame_set_.end() ||
+        std::find(collider_frame_set_.begin(), collider_frame_set_.end(), false) != collider_frame_set_.end())
+        return fail(KHS_ERROR_INVALID_STATE, "animation has missing frames");
+    animation_ready_ = true;
+    current_frame_ = 0;
+    return KHS_OK;
+}
+
+KhsResult Engine::fail(KhsResult r, const std::string &message)
+{
+    error_ = message;
+    step_stats_.phase = KHS_PHASE_FAILED;
+    progress_phase_.store(KHS_PHASE_FAILED);
+    return r;
+}
+
+void Engine::clear_failure()
+{
+    failure_ = {};
+    failure_.struct_size = sizeof(failure_);
+    failure_.strand_index = kNone;
+    failure_.element_index = kNone;
+    failure_.collider_triangle_index = kNone;
+}
+
+void Engine::set_failure_context(uint32_t kind, uint32_t frame, uint32_t sub, uint32_t attempted, uint32_t maximum,
+                                 uint32_t attempts)
+{
+    failure_.kind = kind; failure_.frame_index = frame; failure_.substep = sub;
+    failure_.requested_substeps = desc_.substeps; failure_.attempted_substeps = attempted;
+    failure_.maximum_substeps = maximum; failure_.adaptive_attempt_count = attempts;
+}
+
+KhsProgress Engine::progress() const
+{
+    KhsProgress p{};
+    p.struct_size = sizeof(p);
+    p.phase = progress_phase_.load(); p.frame_index = progress_frame_.load(); p.frame_count = progress_frame_count_.load();
+    p.substep = progress_substep_.load(); p.substep_count = progress_substep_count_.load();
+    p.nonlinear_iteration = progress_iteration_.load(); p.nonlinear_iteration_limit = desc_.newton_iterations;
+    p.cancelled = cancel_.load() ? 1u : 0u;
+    p.frame_elapsed_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - frame_clock_).count();
+    return p;
+}
+
+EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
+{
+    Impl &I = *d_;
+    const View &v = I.v;
+    const bool trial = alpha >= 0.0;
+    I.launch(gradient ? "k_node_eval_grad" : "k_node_eval_energy", k_node_eval, grid_for(v.N), kBlock, v, gradient ? 1 : 0,
+             trial ? 1 : 0, trial ? alpha : 0.0, dt);
+    I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", k_elem_eval, grid_for(v.E), kBlock, v, gradient ? 1 : 0);
+    if (gradient) I.launch("k_node_sum", k_node_sum, grid_for(v.N), kBlock, v);
+    I.launch("k_reduce_eval", k_reduce_eval, kPartials, kBlock, v, gradient ? 1 : 0);
+    I.launch("k_final_eval", k_final_eval, 1, kBlock, v);
+    I.check();
+    I.sync();
+    const Mailbox &mb = *I.mail_host;
+    EvalStats s;
+    s.objective = mb.objective; s.elastic = mb.elastic; s.contact = mb.contact; s.kinetic = mb.kinetic;
+    s.minimum_gap = mb.minimum_gap; s.grad_norm2 = mb.grad_norm2; s.candidates = mb.candidates; s.active = mb.active;
+    s.feasible = mb.feasible;
+    return s;
+}
+
+void Engine::limit_direction(double max_translation)
+{
+    Impl &I = *d_;
+    if (max_translation > trust_radius_) {
+        I.launch("k_scale", k_scale, grid_for(6 * size_t(I.v.N)), kBlock, I.v, trust_radius_ / max_translation);
+    }
+}
+
+void Engine::make_steepest()
+{
+    Impl &I = *d_;
+    I.launch("k_steepest", k_steepest, grid_for(6 * size_t(I.v.N)), kBlock, I.v);
+    I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
+    I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
+    I.check();
+    I.sync();
+    limit_direction(I.mail_host->max_translation);
+}
+
+bool Engine::make_direction(KhsxSubstepRecord &rec)
+{
+    Impl &I = *d_;
+    const unsigned warps = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
+    I.launch("k_block_solve", k_block_solve, (warps + 3) / 4, 128, I.v);
+    I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
+    I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
+    I.check();
+    I.sync();
+    const Mailbox &mb = *I.mail_host;
+    const bool used = !mb.solve_failed && mb.slope < 0 && std::isfinite(mb.slope);
+    if (!used) {
+        ++rec.steepest_fallbacks;
+        make_steepest();
+        return false;
+    }
+    limit_direction(mb.max_translation);
+    return true;
+}
+
+KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
+{
+    Impl &I = *d_;
+    const View &v = I.v;
+    I.launch("k_precond", k_precond, grid_for(v.N), kBlock, v, dt);
+    EvalStats current = evaluate(true, dt, -1.0);
+    if (!current.feasible) return fail(KHS_ERROR_NOT_CONVERGED, "state is outside the barrier feasible region");
+    const double initial = std::sqrt(current.grad_norm2);
+    step_stats_.initial_residual_norm = std::fmax(step_stats_.initial_residual_norm, initial);
+    const double dof = 6.0 * double(v.N);
+    for (uint32_t it = 0; it <= desc_.newton_iterations; ++it) {
+        progress_iteration_.store(it);
+        if (cancel_.load()) return fail(KHS_ERROR_INVALID_STATE, "solve cancelled");
+        const double residual = std::sqrt(current.grad_norm2);
+        const double relative = residual / std::fmax(initial, 1e-30);
+        step_stats_.final_residual_norm = residual;
+        step_stats_.relative_residual_norm = relative;
+        step_stats_.minimum_gap = std::fmin(step_stats_.minimum_gap, current.minimum_gap);
+        step_stats_.contact_candidate_count += current.candidates;
+        step_stats_.active_contact_count += current.active;
+        step_stats_.kinetic_energy = current.kinetic;
+        step_stats_.elastic_energy = current.elastic;
+        step_stats_.contact_energy = current.contact;
+        step_stats_.friction_energy = 0.0;
+        rec.final_residual_norm = residual;
+        rec.minimum_gap = std::fmin(rec.minimum_gap, current.minimum_gap);
+        rec.contact_candidates += current.candidates;
+        rec.active_contacts += current.active;
+        if (residual <= std::fmax(desc_.absolute_tolerance, 1.0e-5 * std::sqrt(dof)) ||
+            relative <= std::fmax(desc_.relative_tolerance, 1.0e-4)) {
+            I.launch("k_update_velocity", k_update_velocity, grid_for(v.N), kBlock, v, 1.0 / dt);
+            return KHS_OK;
+        }
+        if (it == desc_.newton_iterations) break;
+        progress_phase_.store(KHS_PHASE_LINEAR_SOLVE);
+        bool block_direction = make_direction(rec);
+        ++step_stats_.linear_solves;
+        KHS_CUDA(cudaMemcpyAsync(v.q_base, v.q, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+        bool accepted = false;
+        double alpha = 1.0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            // Slope of the (possibly scaled) direction, and the CCD bound.
+            I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, v);
+            if (v.has_collider) {
+                progress_phase_.store(KHS_PHASE_CCD);
+                I.launch("k_ccd", k_ccd, grid_for(v.E), kBlock, v);
+            }
+            I.launch("k_final_dir", k_final_dir, 1, kBlock, v);
+            I.check();
+            I.sync();
+            const double slope = I.mail_host->slope;
+            alpha = 1.0;
+            if (v.has_collider) {
+                unsigned long long bits = I.mail_host->ccd_bits;
+                double lim;
+                std::memcpy(&lim, &bits, sizeof(lim));
+                alpha = lim;
+                if (alpha < 1.0) alpha *= 0.9;
+                step_stats_.ccd_step_limit = std::fmin(step_stats_.ccd_step_limit, alpha);
+            }
+            accepted = false;
+            progress_phase_.store(KHS_PHASE_LINE_SEARCH);
+            if (alpha >= desc_.minimum_line_search_step)
+                for (uint32_t s = 0; s < desc_.line_search_iterations; ++s) {
+                    const EvalStats trial = evaluate(false, dt, alpha);
+                    ++step_stats_.line_search_evaluations;
+                    ++rec.line_search_evaluations;
+                    if (trial.feasible && std::isfinite(trial.objective) &&
+                        trial.objective <= current.objective + 1e-4 * alpha * slope) {
+                        accepted = true;
+                        break;
+                    }
+                    alpha *= 0.5;
+                    if (alpha < desc_.minimum_line_search_step) break;
+                }
+            if (accepted) break;
+            if (!block_direction) break;
+            KHS_CUDA(cudaMemcpyAsync(v.q, v.q_base, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+            ++rec.steepest_fallbacks;
+            make_steepest();
+            block_direction = false;
+        }
+        if (!accepted) {
+            KHS_CUDA(cudaMemcpyAsync(v.q, v.q_base, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+            I.sync();
+            return fail(KHS_ERROR_NOT_CONVERGED, "Gauss-Newton line search failed");
+        }
+        current = evaluate(true, dt, -1.0);
+        const double dnorm = std::sqrt(I.mail_host->dir_norm2);
+        step_stats_.increment_norm = alpha * dnorm;
+        step_stats_.accepted_step_length = alpha;
+        ++step_stats_.newton_iterations;
+        ++rec.newton_iterations;
+        progress_phase_.store(KHS_PHASE_ASSEMBLING);
+        if (step_stats_.increment_norm / std::sqrt(dof) <= 2.0 * desc_.increment_tolerance) {
+            I.launch("k_update_velocity", k_update_velocity, grid_for(v.N), kBlock, v, 1.0 / dt);
+            return KHS_OK;
+        }
+    }
+    I.launch("k_update_velocity", k_update_velocity, grid_for(v.N), kBlock, v, 1.0 / dt);
+    return KHS_OK;
+}
+
+KhsResult Engine::run_frame(double frame_dt, const double *root_a, const double *rot_a, const double *root_b,
+                            const double *rot_b, const double *col_a, const double *col_b, uint32_t frame,
+                            uint32_t frame_count)
+{
+    Impl &I = *d_;
+    View &v = I.v;
+    if (!(frame_dt > 0 && std::isfinite(frame_dt))) return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid time step");
+    cancel_.store(false);
+    clear_failure();
+    frame_clock_ = std::chrono::steady_clock::now();
+    progress_frame_.store(frame); progress_frame_count_.store(frame_count); progress_iteration_.store(0);
+    const size_t q_bytes = 6 * size_t(v.N) * 8, c_bytes = 3 * size_t(v.V) * 8;
+    KHS_CUDA(cudaEventRecord(I.ev_begin, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.q_snap, v.q, q_bytes, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.v_snap, v.v, q_bytes, cudaMemcpyDeviceToDevice, I.stream));
+    // Keep the frame's start collider: for khsStep it aliases the
+    // frame-start buffer that is rewritten on success.
+    if (v.V) {
+        KHS_CUDA(cudaMemcpyAsync(I.col_a_copy, col_a, c_bytes, cudaMemcpyDeviceToDevice, I.stream));
+        if (col_a != I.col_frame_start)
+            KHS_CUDA(cudaMemcpyAsync(I.col_frame_start, col_a, c_bytes, cudaMemcpyDeviceToDevice, I.stream));
+    }
+    uint32_t substeps = desc_.substeps;
+    const uint32_t maximum = v.has_collider ? desc_.maximum_substeps : desc_.substeps;
+    uint32_t attempts = 0;
+    for (;;) {
+        ++attempts;
+        KHS_CUDA(cudaMemcpyAsync(v.q, I.q_snap, q_bytes, cudaMemcpyDeviceToDevice, I.stream));
+        KHS_CUDA(cudaMemcpyAsync(v.v, I.v_snap, q_bytes, cudaMemcpyDeviceToDevice, I.stream));
+        clear_failure();
+        error_.clear();
+        records_.clear();
+        progress_phase_.store(KHS_PHASE_ASSEMBLING);
+        progress_substep_count_.store(substeps);
+        progress_iteration_.store(0);
+        step_stats_ = {};
+        step_stats_.struct_size = sizeof(step_stats_);
+        step_stats_.substeps = substeps;
+        step_stats_.minimum_gap = std::numeric_limits<double>::infinity();
+        step_stats_.ccd_step_limit = 1.0;
+        if (v.V) KHS_CUDA(cudaMemcpyAsync(v.col_cur, I.col_a_copy, c_bytes, cudaMemcpyDeviceToDevice, I.stream));
+        const double dt = frame_dt / substeps;
+        bool crossed = false;
+        KhsResult result = KHS_OK;
+        for (uint32_t sub = 1; sub <= substeps; ++sub) {
+            progress_substep_.store(sub);
+            progress_iteration_.store(0);
+            KhsxSubstepRecord rec{};
+            rec.struct_size = sizeof(rec);
+            rec.substep = sub;
+            rec.minimum_gap = std::numeric_limits<double>::infinity();
+            const double f = double(sub) / substeps;
+            I.launch("k_begin_substep", k_begin_substep, grid_for(v.N), kBlock, v, root_a, rot_a, root_b, rot_b, f, dt);
+            if (v.has_collider) {
+                I.launch("k_collider_interp", k_collider_interp, grid_for(v.V), kBlock, v, I.col_a_copy, col_b, f);
+                I.launch("k_refit", k_refit, grid_for(v.L), kBlock, v, 1);
+                progress_phase_.store(KHS_PHASE_CCD);
+                I.launch("k_sweep", k_sweep, grid_for(v.E), kBlock, v);
+                I.launch("k_sweep_record", k_sweep_record, 1, 1, v);
+                I.check();
+                I.sync();
+                if (I.mail_host->sweep_fail != kNone) {
+                    const SweepRecord &sr = *I.sweep_host;
+                    set_failure_context(KHS_FAILURE_MOVING_COLLIDER_SWEEP, frame, sub, substeps, maximum, attempts);
+                    if (sr.claimed) {
+                        failure_.strand_index = sr.strand; failure_.element_index = sr.element;
+                        failure_.collider_triangle_index = sr.triangle;
+                        failure_.distance = sr.distance; failure_.required_distance = sr.required;
+                        failure_.clearance = sr.clearance; failure_.collider_substep_displacement = sr.displacement;
+                        failure_.collider_frame_displacement = sr.displacement * substeps;
+                        failure_.hair_start = {sr.hair_start[0], sr.hair_start[1], sr.hair_start[2]};
+                        failure_.hair_end = {sr.hair_end[0], sr.hair_end[1], sr.hair_end[2]};
+                        failure_.collider_point = {sr.collider_point[0], sr.collider_point[1], sr.collider_point[2]};
+                    }
+                    crossed = true;
+                    break;
+                }
+                I.launch("k_refit", k_refit, grid_for(v.L), kBlock, v, 0);
+            }
+            progress_phase_.store(KHS_PHASE_ASSEMBLING);
+            result = optimize_substep(dt, rec);
+            records_.push_back(rec);
+            if (result != KHS_OK) {
+                if (!cancel_.load()) {
+                    const uint32_t kind = error_.find("outside the barrier") != std::string::npos ? KHS_FAILURE_BARRIER_INFEASIBLE
+                                                                                                   : KHS_FAILURE_NONLINEAR_SOLVE;
+                    set_failure_context(kind, frame, sub, substeps, maximum, attempts);
+                }
+                break;
+            }
+            if (v.has_collider && material_.friction > 0.0) {
+                I.launch("k_friction", k_friction, grid_for(v.E), kBlock, v, dt);
+                I.launch("k_friction_apply", k_friction_apply, grid_for(v.N), kBlock, v);
+            }
+            ++step_stats_.converged_substeps;
+        }
+        if (!crossed && result == KHS_OK) break;
+        KHS_CUDA(cudaMemcpyAsync(v.q, I.q_snap, q_bytes, cudaMemcpyDeviceToDevice, I.stream));
+        KHS_CUDA(cudaMemcpyAsync(v.v, I.v_snap, q_bytes, cudaMemcpyDeviceToDevice, I.stream));
+        I.sync();
+        if (cancel_.load()) return result;
+        if (substeps >= maximum) {
+            if (crossed) return fail(KHS_ERROR_NOT_CONVERGED, "animated collider crossed hair after adaptive substepping");
+            return result;
+        }
+        substeps = std::min(maximum, substeps * 2);
+    }
+    if (!animation_ready_) {
+        KHS_CUDA(cudaMemcpyAsync(I.root_cur_x, I.root_pend_x, 3 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+        KHS_CUDA(cudaMemcpyAsync(I.root_cur_r, I.root_pend_r, 3 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+        if (v.V) KHS_CUDA(cudaMemcpyAsync(I.col_frame_start, I.col_pending, c_bytes, cudaMemcpyDeviceToDevice, I.stream));
+    }
+    clear_failure();
+    step_stats_.phase = KHS_PHASE_FINISHED;
+    progress_phase_.store(KHS_PHASE_FINISHED);
+    KHS_CUDA(cudaEventRecord(I.ev_end, I.stream));
+    KHS_CUDA(cudaEventSynchronize(I.ev_end));
+    float ms = 0;
+    KHS_CUDA(cudaEventElapsedTime(&ms, I.ev_begin, I.ev_end));
+    gpu_stats_.last_frame_milliseconds = ms;
+    error_.clear();
+    return KHS_OK;
+}
+
+KhsResult Engine::step(double frame_dt)
+{
+    Impl &I = *d_;
+    return run_frame(frame_dt, I.root_cur_x, I.root_cur_r, I.root_pend_x, I.root_pend_r, I.col_frame_start, I.col_pending, 0, 0);
+}
+
+KhsResult Engine::step_animation_frame(uint32_t frame, double frame_dt)
+{
+    Impl &I = *d_;
+    if (!animation_ready_ || frame >= animation_frames_) return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid animation frame index");
+    if (frame == 0) { current_frame_ = 0; return KHS_OK; }
+    if (frame != current_frame_ + 1) return fail(KHS_ERROR_INVALID_STATE, "animation frames must be stepped in order");
+    const size_t N3 = 3 * size_t(I.v.N), V3 = 3 * size_t(I.v.V);
+    const uint32_t a = frame - 1, b = frame;
+    const KhsResult r = run_frame(frame_dt, I.anim_root_x + a * N3, I.anim_root_r + a * N3, I.anim_root_x + b * N3,
+                                  I.anim_root_r + b * N3, I.v.V ? I.anim_col + a * V3 : nullptr,
+                                  I.v.V ? I.anim_col + b * V3 : nullptr, frame, animation_frames_);
+    if (r == KHS_OK) current_frame_ = frame;
+    return r;
+}
+
+namespace {
+struct CheckpointHeader {
+    uint64_t magic;
+    uint32_t abi_version;
+    uint32_t animation_frame;
+    uint64_t dof_count;
+};
+}  // namespace
+
+uint64_t Engine::checkpoint_size() const
+{
+    if (!initialized_ || !animation_ready_) return 0;
+    return sizeof(CheckpointHeader) + 2 * uint64_t(6) * d_->v.N * sizeof(double);
+}
+
+KhsResult Engine::save_checkpoint(void *data, uint64_t capacity)
+{
+    Impl &I = *d_;
+    const uint64_t required = checkpoint_size();
+    if (!data || !required || capacity < required) return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid checkpoint output buffer");
+    CheckpointHeader h{kCheckpointMagic, KHS_ABI_VERSION, current_frame_, uint64_t(6) * I.v.N};
+    auto *out = static_cast<unsigned char *>(data);
+    std::memcpy(out, &h, sizeof(h));
+    const size_t qb = 6 * size_t(I.v.N) * 8;
+    KHS_CUDA(cudaMemcpyAsync(out + sizeof(h), I.v.q, qb, cudaMemcpyDeviceToHost, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(out + sizeof(h) + qb, I.v.v, qb, cudaMemcpyDeviceToHost, I.stream));
+    I.sync();
+    error_.clear();
+    return KHS_OK;
+}
+
+KhsResult Engine::restore_checkpoint(const void *data, uint64_t size)
+{
+    Impl &I = *d_;
+    const uint64_t required = checkpoint_size();
+    if (!data || !required || size != required) return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid checkpoint size");
+    CheckpointHeader h{};
+    std::memcpy(&h, data, sizeof(h));
+    if (h.magic != kCheckpointMagic || h.abi_version != KHS_ABI_VERSION || h.dof_count != uint64_t(6) * I.v.N ||
+        h.animation_frame >= animation_frames_)
+        return fail(KHS_ERROR_INVALID_ARGUMENT, "checkpoint does not match this solver");
+    const auto *in = static_cast<const unsigned char *>(data);
+    const size_t qb = 6 * size_t(I.v.N) * 8;
+    KHS_CUDA(cudaMemcpyAsync(I.v.q, in + sizeof(h), qb, cudaMemcpyHostToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.v.v, in + sizeof(h) + qb, qb, cudaMemcpyHostToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.v.q_old, I.v.q, qb, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.q_snap, I.v.q, qb, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.v_snap, I.v.v, qb, cudaMemcpyDeviceToDevice, I.stream));
+    I.sync();
+    current_frame_ = h.animation_frame;
+    cancel_.store(false);
+    progress_frame_.store(h.animation_frame);
+    progress_substep_.store(0); progress_substep_count_.store(0); progress_iteration_.store(0);
+    progress_phase_.store(KHS_PHASE_FINISHED);
+    step_stats_ = {};
+    step_stats_.struct_size = sizeof(step_stats_);
+    step_stats_.phase = KHS_PHASE_FINISHED;
+    clear_failure();
+    error_.clear();
+    return KHS_OK;
+}
+
+KhsResult Engine::copy_original_positions(KhsVec3 *out, uint32_t capacity) const
+{
+    Impl &I = *d_;
+    if (!out || capacity < I.original_count) return KHS_ERROR_INVALID_ARGUMENT;
+    if (!I.original_count) return KHS_OK;
+    I.launch("k_gather", k_gather, grid_for(I.original_count), kBlock, I.v.q, I.mapping_dev, I.original_count, I.mapping_gather_out);
+    KHS_CUDA(cudaGetLastError());
+    KHS_CUDA(cudaMemcpyAsync(out, I.mapping_gather_out, size_t(I.original_count) * 24, cudaMemcpyDeviceToHost, I.stream));
+    I.sync();
+    return KHS_OK;
+}
+
+KhsResult Engine::copy_internal_positions(KhsVec3 *out, uint32_t capacity) const
+{
+    Impl &I = *d_;
+    if (!out || capacity < I.v.N) return KHS_ERROR_INVALID_ARGUMENT;
+    I.launch("k_gather", k_gather, grid_for(I.v.N), kBlock, I.v.q, nullptr, I.v.N, I.mapping_gather_out);
+    KHS_CUDA(cudaGetLastError());
+    KHS_CUDA(cudaMemcpyAsync(out, I.mapping_gather_out, size_t(I.v.N) * 24, cudaMemcpyDeviceToHost, I.stream));
+    I.sync();
+    return KHS_OK;
+}
+
+KhsResult Engine::copy_state(double *q, double *v, uint64_t capacity) const
+{
+    Impl &I = *d_;
+    const size_t dof = 6 * size_t(I.v.N);
+    if (capacity < dof) return KHS_ERROR_INVALID_ARGUMENT;
+    if (q) KHS_CUDA(cudaMemcpyAsync(q, I.v.q, dof * 8, cudaMemcpyDeviceToHost, I.stream));
+    if (v) KHS_CUDA(cudaMemcpyAsync(v, I.v.v, dof * 8, cudaMemcpyDeviceToHost, I.stream));
+    I.sync();
+    return KHS_OK;
+}
+
+KhsResult Engine::query_contacts(const double *q, uint64_t dof, KhsxContactRecord *out, uint32_t capacity)
+{
+    Impl &I = *d_;
+    if (!q || dof < 6 * uint64_t(I.v.N) || !out || capacity < I.v.E) return KHS_ERROR_INVALID_ARGUMENT;
+    KHS_CUDA(cudaMemcpyAsync(I.v.q_base, q, 6 * size_t(I.v.N) * 8, cudaMemcpyHostToDevice, I.stream));
+    I.launch("k_contact_query", k_contact_query, grid_for(I.v.E), kBlock, I.v, I.v.q_base);
+    KHS_CUDA(cudaGetLastError());
+    return copy_contact_records(out, capacity);
+}
+
+KhsResult Engine::copy_contact_records(KhsxContactRecord *out, uint32_t capacity) const
+{
+    Impl &I = *d_;
+    const size_t E = I.v.E;
+    if (!out || capacity < E) return KHS_ERROR_INVALID_ARGUMENT;
+    std::vector<uint32_t> cand(E), tri(E);
+    std::vector<uint8_t> flags(E);
+    std::vector<double> gap(E);
+    if (E) {
+        KHS_CUDA(cudaMemcpyAsync(cand.data(), I.v.c_cand, E * 4, cudaMemcpyDeviceToHost, I.stream));
+        KHS_CUDA(cudaMemcpyAsync(tri.data(), I.v.c_tri, E * 4, cudaMemcpyDeviceToHost, I.stream));
+        KHS_CUDA(cudaMemcpyAsync(flags.data(), I.v.c_flags, E, cudaMemcpyDeviceToHost, I.stream));
+        KHS_CUDA(cudaMemcpyAsync(gap.data(), I.v.c_gap, E * 8, cudaMemcpyDeviceToHost, I.stream));
+        I.sync();
+    }
+    for (size_t e = 0; e < E; ++e) {
+        const bool closest = flags[e] & kFlagClosest;
+        out[e] = KhsxContactRecord{cand[e], closest ? tri[e] : kNone, (flags[e] & kFlagActive) ? 1u : 0u, 0u,
+                                   closest ? gap[e] : std::numeric_limits<double>::infinity()};
+    }
+    return KHS_OK;
+}
+
+void Engine::set_profiling(bool on)
+{
+    Impl &I = *d_;
+    I.sync();
+    I.profiling = on;
+}
+
+std::vector<KernelTiming> Engine::kernel_timings() const
+{
+    Impl &I = *d_;
+    I.sync();
+    std::vector<KernelTiming> out;
+    for (const auto &k : I.kstats) out.push_back({k.name, k.launches, k.ms});
+    return out;
+}
+
+void Engine::reset_kernel_timings()
+{
+    Impl &I = *d_;
+    I.sync();
+    I.kstats.clear();
+}
+
+uint64_t Engine::kernel_launches() const { return d_->launches; }
+
+bool query_device(KhsGpuInfo &info, std::string &error)
+{
+    std::memset(&info, 0, sizeof(info));
+    info.struct_size = sizeof(info);
+    int count = 0;
+    const cudaError_t r = cudaGetDeviceCount(&count);
+    if (r != cudaSuccess || count < 1) {
+        error = r == cudaSuccess ? "no CUDA GPU found" : cudaGetErrorString(r);
+        cudaGetLastError();
+        return false;
+    }
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, 0) != cudaSuccess) { error = "cannot query the CUDA device"; return false; }
+    info.available = 1;
+    info.device_ordinal = 0;
+    info.compute_capability_major = uint32_t(prop.major);
+    info.compute_capability_minor = uint32_t(prop.minor);
+    info.total_vram_bytes = prop.totalGlobalMem;
+    std::strncpy(info.device_name, prop.name, sizeof(info.device_name) - 1);
+    return true;
+}
+
+}  // namespace khs

@@ -1,0 +1,624 @@
+// Host-side rod model builder (see khs_model.hpp).
+#include "khs_model.hpp"
+
+#include <algorithm>
+#include <limits>
+#include <numeric>
+#include <sstream>
+#include <unordered_map>
+
+namespace khs {
+namespace {
+
+constexpr double kPiHost = 3.14159265358979323846;
+
+inline Vec mk(double x, double y, double z) { Vec v; v.x = x; v.y = y; v.z = z; return v; }
+inline Vec add(Vec a, Vec b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline Vec sub(Vec a, Vec b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline Vec mul(Vec a, double s) { return mk(a.x * s, a.y * s, a.z * s); }
+inline Vec divs(Vec a, double s) { return mk(a.x / s, a.y / s, a.z / s); }
+inline double dot(Vec a, Vec b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline Vec cross(Vec a, Vec b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline double sq(Vec a) { return dot(a, a); }
+inline double len(Vec a) { return std::sqrt(sq(a)); }
+inline double comp(Vec a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+inline Vec vmin(Vec a, Vec b) { return mk(std::fmin(a.x, b.x), std::fmin(a.y, b.y), std::fmin(a.z, b.z)); }
+inline Vec vmax(Vec a, Vec b) { return mk(std::fmax(a.x, b.x), std::fmax(a.y, b.y), std::fmax(a.z, b.z)); }
+inline bool finite(Vec a) { return std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(a.z); }
+// Unit vector; a zero vector stays zero (Eigen normalized()).
+inline Vec unit(Vec a)
+{
+    const double n2 = sq(a);
+    return n2 > 0.0 ? divs(a, std::sqrt(n2)) : a;
+}
+// (1 - t) a + t b with the reference's evaluation order.
+inline Vec lerp(Vec a, Vec b, double t) { return add(mul(a, 1.0 - t), mul(b, t)); }
+
+inline Vec column(const Mat &m, int c) { return mk(m.m[c], m.m[3 + c], m.m[6 + c]); }
+inline Mat from_columns(Vec a, Vec b, Vec c)
+{
+    Mat r;
+    r.m[0] = a.x; r.m[1] = b.x; r.m[2] = c.x;
+    r.m[3] = a.y; r.m[4] = b.y; r.m[5] = c.y;
+    r.m[6] = a.z; r.m[7] = b.z; r.m[8] = c.z;
+    return r;
+}
+inline Mat times_transpose(const Mat &a, const Mat &b)  // a * b^T
+{
+    Mat r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            r.m[3 * i + j] = (a.m[3 * i] * b.m[3 * j] + a.m[3 * i + 1] * b.m[3 * j + 1]) + a.m[3 * i + 2] * b.m[3 * j + 2];
+    return r;
+}
+inline Mat transpose_times(const Mat &a, const Mat &b)  // a^T * b
+{
+    Mat r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            r.m[3 * i + j] = (a.m[i] * b.m[j] + a.m[3 + i] * b.m[3 + j]) + a.m[6 + i] * b.m[6 + j];
+    return r;
+}
+
+// Regularised Cayley rotation vector (math.hpp:14-24).
+Vec cayley(const Mat &q)
+{
+    const Vec v = mk((q.m[7] - q.m[5]) * 0.5, (q.m[2] - q.m[6]) * 0.5, (q.m[3] - q.m[1]) * 0.5);
+    const double c = (((q.m[0] + q.m[4]) + q.m[8]) - 1.0) * 0.5;
+    const double s = 2.0 / (1.0 + c + 1.0e-12);
+    return mk(s * v.x, s * v.y, s * v.z);
+}
+
+// Frame with the tangent as third column, first column from the hint
+// (math.hpp:26-43).
+Mat tangent_frame(Vec tangent, Vec hint)
+{
+    const Vec d3 = unit(tangent);
+    Vec d1 = sub(hint, mul(d3, dot(hint, d3)));
+    if (sq(d1) < 1.0e-16) {
+        const Vec axis = std::fabs(d3.x) < 0.8 ? mk(1, 0, 0) : mk(0, 1, 0);
+        d1 = sub(axis, mul(d3, dot(axis, d3)));
+    }
+    d1 = unit(d1);
+    const Vec d2 = unit(cross(d3, d1));
+    d1 = unit(cross(d2, d3));
+    return from_columns(d1, d2, d3);
+}
+
+// Any unit vector orthogonal to s, chosen like Eigen's unitOrthogonal.
+Vec orthogonal_unit(Vec s)
+{
+    const double eps = 1e-12;
+    if (!(std::fabs(s.x) <= std::fabs(s.z) * eps) || !(std::fabs(s.y) <= std::fabs(s.z) * eps)) {
+        const double inv = 1.0 / std::sqrt(s.x * s.x + s.y * s.y);
+        return mk(-s.y * inv, s.x * inv, 0.0);
+    }
+    const double inv = 1.0 / std::sqrt(s.y * s.y + s.z * s.z);
+    return mk(0.0, -s.z * inv, s.y * inv);
+}
+
+// Minimal rotation of a director between consecutive tangents
+// (math.hpp:45-58).
+Vec transport(Vec director, Vec from, Vec to)
+{
+    const Vec a = unit(from), b = unit(to);
+    const Vec axis = cross(a, b);
+    const double s = len(axis);
+    const double c = std::clamp(dot(a, b), -1.0, 1.0);
+    if (s < 1.0e-12) {
+        if (c > 0.0) return director;
+        const Vec n = orthogonal_unit(a);
+        return sub(mul(mul(n, 2.0), dot(n, director)), director);
+    }
+    const Vec n = divs(axis, s);
+    return add(add(mul(director, c), mul(cross(n, director), s)), mul(mul(n, dot(n, director)), 1.0 - c));
+}
+
+// Rotation vector of a rotation matrix.  Shepperd's method (J. Guidance and
+// Control 1(3), 1978) gives the quaternion from the largest of its four
+// squared components; the angle is 2 atan2(|v|, |w|) and the axis v/|v|
+// carries the sign of w (the reference goes through Eigen::AngleAxisd,
+// solver.cpp:19-26).
+Vec rotation_vector(const Mat &r)
+{
+    double q[4];  // x y z w
+    const double tr = (r.m[0] + r.m[4]) + r.m[8];
+    if (tr > 0.0) {
+        double s = std::sqrt(tr + 1.0);
+        q[3] = 0.5 * s;
+        s = 0.5 / s;
+        q[0] = (r.m[7] - r.m[5]) * s;
+        q[1] = (r.m[2] - r.m[6]) * s;
+        q[2] = (r.m[3] - r.m[1]) * s;
+    } else {
+        int i = 0;
+        if (r.m[4] > r.m[0]) i = 1;
+        if (r.m[8] > r.m[4 * i]) i = 2;
+        const int j = (i + 1) % 3, k = (j + 1) % 3;
+        double s = std::sqrt(r.m[4 * i] - r.m[4 * j] - r.m[4 * k] + 1.0);
+        q[i] = 0.5 * s;
+        s = 0.5 / s;
+        q[3] = (r.m[3 * k + j] - r.m[3 * j + k]) * s;
+        q[j] = (r.m[3 * j + i] + r.m[3 * i + j]) * s;
+        q[k] = (r.m[3 * k + i] + r.m[3 * i + k]) * s;
+    }
+    double n = std::sqrt((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]);
+    if (!(n != 0.0)) return Vec{};
+    double angle = 2.0 * std::atan2(n, std::fabs(q[3]));
+    if (q[3] < 0.0) n = -n;
+    const Vec axis = mk(q[0] / n, q[1] / n, q[2] / n);
+    if (!std::isfinite(angle) || !finite(axis)) return Vec{};
+    if (angle > kPiHost) angle -= 2.0 * kPiHost;
+    return mul(axis, angle);
+}
+
+// Unit central-difference tangents along one strand (solver.cpp:324-331).
+bool strand_tangents(const std::vector<Vec> &x, uint32_t first, uint32_t count, std::vector<Vec> &t, bool reject_zero)
+{
+    t.resize(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        Vec d;
+        if (k == 0) d = sub(x[first + 1], x[first]);
+        else if (k + 1 == count) d = sub(x[first + k], x[first + k - 1]);
+        else d = sub(x[first + k + 1], x[first + k - 1]);
+        if (reject_zero && sq(d) < 1.0e-24) return false;
+        t[k] = unit(d);
+    }
+    return true;
+}
+
+// ---- BVH construction (two flavours of the same median split) ----------
+
+struct TreeNode {
+    Vec lo, hi;
+    uint32_t begin = 0, count = 0;
+    int left = -1, right = -1;
+};
+
+struct TreeBuilder {
+    const std::vector<Vec> &v;
+    const std::vector<uint32_t> &tri;
+    bool device_flavour;
+    std::vector<TreeNode> nodes;
+    std::vector<uint32_t> order;
+
+    Vec vert(uint32_t t, int c) const { return v[tri[3 * t + c]]; }
+    // Device flavour multiplies by 1/3 (cuda_backend.cu:40,303); host
+    // flavour divides each component by 3 (solver.cpp:65,78-79).
+    double centroid(uint32_t t, int axis) const
+    {
+        const Vec s = add(add(vert(t, 0), vert(t, 1)), vert(t, 2));
+        return device_flavour ? comp(s, axis) * (1.0 / 3.0) : comp(s, axis) / 3.0;
+    }
+    int build(uint32_t begin, uint32_t end)
+    {
+        const int idx = int(nodes.size());
+        nodes.push_back({});
+        const double big = device_flavour ? 1e300 : std::numeric_limits<double>::infinity();
+        Vec lo = mk(big, big, big), hi = mk(-big, -big, -big), cl = lo, cu = hi;
+        for (uint32_t k = begin; k < end; ++k) {
+            const uint32_t t = order[k];
+            const Vec a = vert(t, 0), b = vert(t, 1), c = vert(t, 2);
+            lo = vmin(lo, vmin(a, vmin(b, c)));
+            hi = vmax(hi, vmax(a, vmax(b, c)));
+            const Vec s = add(add(a, b), c);
+            const Vec ce = device_flavour ? mul(s, 1.0 / 3.0) : divs(s, 3.0);
+            cl = vmin(cl, ce);
+            cu = vmax(cu, ce);
+        }
+        nodes[idx].lo = lo; nodes[idx].hi = hi;
+        nodes[idx].begin = begin; nodes[idx].count = end - begin;
+        if (end - begin <= 8) return idx;
+        const Vec span = sub(cu, cl);
+        int axis;
+        if (device_flavour) axis = span.y > span.x ? (span.z > span.y ? 2 : 1) : (span.z > span.x ? 2 : 0);
+        else { axis = 0; if (span.y > comp(span, axis)) axis = 1; if (span.z > comp(span, axis)) axis = 2; }
+        const uint32_t mid = begin + (end - begin) / 2;
+        std::nth_element(order.begin() + begin, order.begin() + mid, order.begin() + end,
+                         [&](uint32_t l, uint32_t r) { return centroid(l, axis) < centroid(r, axis); });
+        const int left = build(begin, mid);
+        const int right = build(mid, end);
+        nodes[idx].left = left; nodes[idx].right = right; nodes[idx].count = 0;
+        return idx;
+    }
+    void run()
+    {
+        order.resize(tri.size() / 3);
+        std::iota(order.begin(), order.end(), 0u);
+        nodes.clear();
+        if (!order.empty()) build(0, uint32_t(order.size()));
+    }
+};
+
+inline bool boxes_touch(Vec al, Vec au, Vec bl, Vec bu, double p)
+{
+    return al.x <= bu.x + p && bl.x <= au.x + p && al.y <= bu.y + p && bl.y <= au.y + p && al.z <= bu.z + p &&
+           bl.z <= au.z + p;
+}
+
+// ---- host closest-distance (geometry.hpp flavour) -----------------------
+
+Vec triangle_point(Vec p, Vec a, Vec b, Vec c)
+{
+    const Vec ab = sub(b, a), ac = sub(c, a), ap = sub(p, a);
+    const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.0 && d2 <= 0.0) return a;
+    const Vec bp = sub(p, b);
+    const double d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0.0 && d4 <= d3) return b;
+    const double vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) return add(a, mul(ab, d1 / (d1 - d3)));
+    const Vec cp = sub(p, c);
+    const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.0 && d5 <= d6) return c;
+    const double vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) return add(a, mul(ac, d2 / (d2 - d6)));
+    const double va = d3 * d6 - d5 * d4;
+    if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0)
+        return add(b, mul(sub(c, b), (d4 - d3) / ((d4 - d3) + (d5 - d6))));
+    const double inv = 1.0 / (va + vb + vc);
+    return add(add(a, mul(ab, vb * inv)), mul(ac, vc * inv));
+}
+
+double segment_segment(Vec p1, Vec q1, Vec p2, Vec q2)
+{
+    const Vec d1 = sub(q1, p1), d2 = sub(q2, p2), r = sub(p1, p2);
+    const double a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+    double s = 0.0, t = 0.0;
+    if (!(a <= 1e-14 && e <= 1e-14)) {
+        if (a <= 1e-14) t = std::clamp(f / e, 0.0, 1.0);
+        else {
+            const double c = dot(d1, r);
+            if (e <= 1e-14) s = std::clamp(-c / a, 0.0, 1.0);
+            else {
+                const double b = dot(d1, d2), den = a * e - b * b;
+                if (den != 0.0) s = std::clamp((b * f - c * e) / den, 0.0, 1.0);
+                t = (b * s + f) / e;
+                if (t < 0.0) { t = 0.0; s = std::clamp(-c / a, 0.0, 1.0); }
+                else if (t > 1.0) { t = 1.0; s = std::clamp((b - c) / a, 0.0, 1.0); }
+            }
+        }
+    }
+    return len(sub(add(p1, mul(d1, s)), add(p2, mul(d2, t))));
+}
+
+bool segment_crosses(Vec p0, Vec p1, Vec a, Vec b, Vec c)
+{
+    const Vec d = sub(p1, p0), e1 = sub(b, a), e2 = sub(c, a), h = cross(d, e2);
+    const double det = dot(e1, h);
+    if (std::fabs(det) < 1.0e-14) return false;
+    const double inv = 1.0 / det;
+    const Vec s = sub(p0, a);
+    const double u = inv * dot(s, h);
+    if (u < 0.0 || u > 1.0) return false;
+    const Vec q = cross(s, e1);
+    const double v = inv * dot(d, q);
+    if (v < 0.0 || u + v > 1.0) return false;
+    const double t = inv * dot(e2, q);
+    return !(t < 0.0 || t > 1.0);
+}
+
+double segment_triangle_distance(Vec p0, Vec p1, Vec a, Vec b, Vec c)
+{
+    if (segment_crosses(p0, p1, a, b, c)) return 0.0;
+    double best = std::min(len(sub(p0, triangle_point(p0, a, b, c))), len(sub(p1, triangle_point(p1, a, b, c))));
+    best = std::min(best, segment_segment(p0, p1, a, b));
+    best = std::min(best, segment_segment(p0, p1, b, c));
+    best = std::min(best, segment_segment(p0, p1, c, a));
+    return best;
+}
+
+bool inside_closed(const Model &m, Vec p)
+{
+    uint32_t hits = 0;
+    const Vec dir = mk(1.0, 0.0000012345, 0.0000023456);
+    for (size_t t = 0; t < m.tri.size() / 3; ++t) {
+        const Vec a = m.collider[m.tri[3 * t]], b = m.collider[m.tri[3 * t + 1]], c = m.collider[m.tri[3 * t + 2]];
+        const Vec e1 = sub(b, a), e2 = sub(c, a), h = cross(dir, e2);
+        const double det = dot(e1, h);
+        if (std::fabs(det) < 1.0e-14) continue;
+        const double inv = 1.0 / det;
+        const Vec s = sub(p, a);
+        const double u = inv * dot(s, h);
+        if (u < 0.0 || u > 1.0) continue;
+        const Vec q = cross(s, e1);
+        const double v = inv * dot(dir, q);
+        if (v < 0.0 || u + v > 1.0) continue;
+        if (inv * dot(e2, q) > 1.0e-12) ++hits;
+    }
+    return (hits & 1u) != 0;
+}
+
+}  // namespace
+
+bool build_rod_model(const SceneInput &in, const KhsSolverDesc &desc, const KhsHairMaterial &material,
+                     Model &m, std::string &error)
+{
+    m = Model{};
+    const uint32_t strand_count = uint32_t(in.offsets.size() - 1);
+    const double hmax = desc.maximum_element_length, zero_tol = 1.0e-12;
+    m.mapping.assign(in.points.size(), 0);
+    auto push_node = [&](Vec x, uint32_t s, NodeBinding b, bool virt) {
+        m.x.push_back(x);
+        m.node_strand.push_back(s);
+        m.binding.push_back(b);
+        m.virtual_extension.push_back(virt ? 1 : 0);
+        return uint32_t(m.x.size() - 1);
+    };
+    for (uint32_t s = 0; s < strand_count; ++s) {
+        const uint32_t begin = in.offsets[s], end = in.offsets[s + 1];
+        const uint32_t first = uint32_t(m.x.size());
+        m.mapping[begin] = push_node(in.points[begin], s, {begin, begin, 0.0}, false);
+        Vec prev = in.points[begin];
+        uint32_t unique = 0, tip_left = begin, tip_right = begin;
+        double rest = 0.0, tip_len = 0.0;
+        Vec tip_dir;
+        for (uint32_t p = begin + 1; p < end; ++p) {
+            const Vec target = in.points[p];
+            const double seg = len(sub(target, prev));
+            if (seg <= zero_tol) {  // zero-length segment: merge (solver.cpp:263-268)
+                m.mapping[p] = uint32_t(m.x.size() - 1);
+                ++m.merged_segments;
+                prev = target;
+                continue;
+            }
+            const uint32_t div = std::max(1u, uint32_t(std::ceil(seg / hmax)));
+            for (uint32_t d = 1; d <= div; ++d) {
+                const double t = double(d) / div;
+                push_node(lerp(prev, target, t), s, {p - 1, p, t}, false);
+            }
+            m.mapping[p] = uint32_t(m.x.size() - 1);
+            prev = target;
+            rest += seg;
+            tip_left = p - 1;
+            tip_right = p;
+            tip_len = seg;
+            tip_dir = divs(sub(target, in.points[p - 1]), seg);
+            ++unique;
+        }
+        if (unique == 0 || m.x.size() - first < 2) {
+            std::ostringstream ss;
+            ss << "strand " << s << " has all points at one position (points " << begin << ".." << (end - 1) << ")";
+            error = ss.str();
+            return false;
+        }
+        if (desc.minimum_dynamic_length > rest + zero_tol) {  // invisible extension (solver.cpp:292-311)
+            const double ext = desc.minimum_dynamic_length - rest;
+            const uint32_t div = std::max(1u, uint32_t(std::ceil(ext / hmax)));
+            const Vec tip = in.points[end - 1];
+            for (uint32_t d = 1; d <= div; ++d) {
+                const double dist = ext * double(d) / div;
+                push_node(add(tip, mul(tip_dir, dist)), s, {tip_left, tip_right, 1.0 + dist / tip_len}, true);
+            }
+            ++m.extension_strands;
+            m.extension_nodes += div;
+            m.extension_length += ext;
+        }
+        const uint32_t count = uint32_t(m.x.size()) - first;
+        const uint32_t fixed = std::min<uint32_t>(desc.fixed_root_nodes, count);
+        m.strand_first.push_back(first);
+        m.strand_count.push_back(count);
+        m.strand_fixed.push_back(fixed);
+    }
+    const size_t n = m.x.size();
+    m.fixed.assign(n, 0);
+    for (size_t s = 0; s < m.strands(); ++s)
+        for (uint32_t k = 0; k < m.strand_fixed[s]; ++k) m.fixed[m.strand_first[s] + k] = 1;
+
+    // Parallel-transported reference frames and rest strains
+    // (solver.cpp:320-356).
+    m.frame.assign(n, Mat{});
+    std::vector<Vec> tangents;
+    for (size_t s = 0; s < m.strands(); ++s) {
+        const uint32_t first = m.strand_first[s], count = m.strand_count[s];
+        strand_tangents(m.x, first, count, tangents, false);
+        Mat f = tangent_frame(tangents[0], mk(1, 0, 0));
+        m.frame[first] = f;
+        for (uint32_t k = 1; k < count; ++k) {
+            f = tangent_frame(tangents[k], transport(column(f, 0), tangents[k - 1], tangents[k]));
+            m.frame[first + k] = f;
+        }
+        for (uint32_t k = 0; k + 1 < count; ++k) {
+            const uint32_t i = first + k, j = first + k + 1;
+            m.elem_i.push_back(i);
+            m.elem_j.push_back(j);
+            m.elem_strand.push_back(uint32_t(s));
+            m.elem_contact.push_back(m.virtual_extension[j] ? 0 : 1);
+            const double L = len(sub(m.x[j], m.x[i]));
+            m.rest_length.push_back(L);
+            const Vec t = divs(sub(m.x[j], m.x[i]), L);
+            const Mat &ri = m.frame[i], &rj = m.frame[j];
+            // 0.5 (Ri^T + Rj^T) t
+            Vec shear;
+            double *out[3] = {&shear.x, &shear.y, &shear.z};
+            for (int r = 0; r < 3; ++r) {
+                const double h0 = 0.5 * (ri.m[r] + rj.m[r]), h1 = 0.5 * (ri.m[3 + r] + rj.m[3 + r]),
+                             h2 = 0.5 * (ri.m[6 + r] + rj.m[6 + r]);
+                *out[r] = (h0 * t.x + h1 * t.y) + h2 * t.z;
+            }
+            m.rest_shear.push_back(shear);
+            m.rest_curvature.push_back(divs(cayley(transpose_times(ri, rj)), L));
+        }
+    }
+    assign_masses(m, material);
+    (void)error;
+    return true;
+}
+
+void assign_masses(Model &m, const KhsHairMaterial &material)
+{
+    const double area = kPiHost * material.radius * material.radius;
+    const double inertia = kPiHost * std::pow(material.radius, 4.0) / 4.0;
+    const double polar = 2.0 * inertia;
+    m.mass.assign(m.nodes(), 0.0);
+    m.rotational_mass.assign(m.nodes(), 0.0);
+    for (size_t e = 0; e < m.elements(); ++e) {
+        const double mass = material.density * area * m.rest_length[e];
+        const double rmass = material.density * (2.0 * inertia + polar) / 3.0 * m.rest_length[e];
+        m.mass[m.elem_i[e]] += 0.5 * mass;
+        m.mass[m.elem_j[e]] += 0.5 * mass;
+        m.rotational_mass[m.elem_i[e]] += 0.5 * rmass;
+        m.rotational_mass[m.elem_j[e]] += 0.5 * rmass;
+    }
+}
+
+bool root_targets(const Model &m, const std::vector<Vec> &points, std::vector<Vec> &pos, std::vector<Vec> &rot)
+{
+    const size_t n = m.nodes();
+    pos.resize(n);
+    rot.assign(n, Vec{});
+    for (size_t k = 0; k < n; ++k) {
+        const NodeBinding &b = m.binding[k];
+        pos[k] = add(mul(points[b.left], 1.0 - b.t), mul(points[b.right], b.t));
+    }
+    std::vector<Vec> tangents;
+    for (size_t s = 0; s < m.strands(); ++s) {
+        const uint32_t first = m.strand_first[s], count = m.strand_count[s];
+        if (!strand_tangents(pos, first, count, tangents, true)) return false;
+        Mat f = tangent_frame(tangents[0], column(m.frame[first], 0));
+        rot[first] = rotation_vector(times_transpose(f, m.frame[first]));
+        for (uint32_t k = 1; k < count; ++k) {
+            f = tangent_frame(tangents[k], transport(column(f, 0), tangents[k - 1], tangents[k]));
+            rot[first + k] = rotation_vector(times_transpose(f, m.frame[first + k]));
+        }
+    }
+    return true;
+}
+
+void collider_topology(Model &m)
+{
+    m.boundary_edges = m.nonmanifold_edges = m.inconsistent_edges = m.inverted_components = 0;
+    struct Use { uint32_t count = 0; int direction = 0; };
+    std::unordered_map<uint64_t, Use> uses;
+    uses.reserve(m.tri.size());
+    for (size_t t = 0; t < m.tri.size() / 3; ++t)
+        for (int e = 0; e < 3; ++e) {
+            const uint32_t a = m.tri[3 * t + e], b = m.tri[3 * t + (e + 1) % 3];
+            Use &u = uses[(uint64_t(std::min(a, b)) << 32) | std::max(a, b)];
+            ++u.count;
+            u.direction += a < b ? 1 : -1;
+        }
+    for (const auto &kv : uses) {
+        if (kv.second.count == 1) ++m.boundary_edges;
+        else if (kv.second.count > 2) ++m.nonmanifold_edges;
+        else if (kv.second.direction != 0) ++m.inconsistent_edges;
+    }
+    m.closed_manifold = m.boundary_edges == 0 && m.nonmanifold_edges == 0 && m.inconsistent_edges == 0;
+    if (m.closed_manifold) {
+        double six_volume = 0.0;
+        for (size_t t = 0; t < m.tri.size() / 3; ++t)
+            six_volume += dot(m.collider[m.tri[3 * t]], cross(m.collider[m.tri[3 * t + 1]], m.collider[m.tri[3 * t + 2]]));
+        if (six_volume < 0.0) m.inverted_components = 1;
+    }
+}
+
+double minimum_gap_host(const Model &m, const KhsHairMaterial &material, uint64_t *candidates)
+{
+    TreeBuilder tb{m.collider, m.tri, false, {}, {}};
+    tb.run();
+    double best = std::numeric_limits<double>::infinity();
+    uint64_t count = 0;
+    const double pad = material.radius + material.collider_offset + material.barrier_distance;
+    std::vector<int> stack;
+    for (size_t e = 0; e < m.elements(); ++e) {
+        const uint32_t i = m.elem_i[e], j = m.elem_j[e];
+        if (m.fixed[i] || !m.elem_contact[e] || tb.nodes.empty()) continue;
+        const Vec lo = vmin(m.x[i], m.x[j]), hi = vmax(m.x[i], m.x[j]);
+        stack.assign(1, 0);
+        while (!stack.empty()) {
+            const TreeNode &nd = tb.nodes[stack.back()];
+            stack.pop_back();
+            if (!boxes_touch(lo, hi, nd.lo, nd.hi, pad)) continue;
+            if (nd.left >= 0) { stack.push_back(nd.left); stack.push_back(nd.right); continue; }
+            for (uint32_t k = nd.begin; k < nd.begin + nd.count; ++k) {
+                const uint32_t t = tb.order[k];
+                const double d = segment_triangle_distance(m.x[i], m.x[j], m.collider[m.tri[3 * t]],
+                                                           m.collider[m.tri[3 * t + 1]], m.collider[m.tri[3 * t + 2]]);
+                best = std::min(best, d - material.radius - material.collider_offset);
+                ++count;
+            }
+        }
+    }
+    if (candidates) *candidates = count;
+    return best;
+}
+
+bool initial_feasibility(const Model &m, const KhsSolverDesc &desc, const KhsHairMaterial &material,
+                         double &minimum_gap, std::string &error)
+{
+    if (m.closed_manifold)
+        for (size_t k = 0; k < m.nodes(); ++k) {
+            if (m.fixed[k] || m.virtual_extension[k]) continue;
+            if (inside_closed(m, m.x[k])) {
+                std::ostringstream ss;
+                ss << "initial intersection: internal node " << k << " lies inside the closed collider";
+                error = ss.str();
+                return false;
+            }
+        }
+    uint64_t candidates = 0;
+    minimum_gap = minimum_gap_host(m, material, &candidates);
+    if (minimum_gap <= desc.minimum_gap) {
+        std::ostringstream ss;
+        ss << "initial intersection or negative gap: minimum gap " << minimum_gap << " m over " << candidates
+           << " candidates";
+        error = ss.str();
+        return false;
+    }
+    return true;
+}
+
+void build_device_bvh(Model &m)
+{
+    TreeBuilder tb{m.collider, m.tri, true, {}, {}};
+    tb.run();
+    FlatBvh &f = m.bvh;
+    f = FlatBvh{};
+    f.order = tb.order;
+    if (tb.nodes.empty()) return;
+    const size_t count = tb.nodes.size();
+    std::vector<uint32_t> slot(count, 0);
+    f.lower.resize(3 * count); f.upper.resize(3 * count);
+    f.escape.resize(count); f.first.resize(count); f.count.resize(count);
+    f.parent.assign(count, -1); f.left_child.assign(count, 0); f.right_child.assign(count, 0);
+    // Right-first preorder: iterative DFS that pushes left below right.
+    struct Item { int tree; int parent_slot; uint32_t depth; };
+    std::vector<Item> stack{{0, -1, 0}};
+    uint32_t next = 0;
+    std::vector<int> tree_of_slot(count, -1);
+    while (!stack.empty()) {
+        const Item it = stack.back();
+        stack.pop_back();
+        const uint32_t s = next++;
+        slot[it.tree] = s;
+        tree_of_slot[s] = it.tree;
+        f.parent[s] = it.parent_slot;
+        f.depth = std::max(f.depth, it.depth);
+        const TreeNode &t = tb.nodes[it.tree];
+        f.lower[3 * s] = t.lo.x; f.lower[3 * s + 1] = t.lo.y; f.lower[3 * s + 2] = t.lo.z;
+        f.upper[3 * s] = t.hi.x; f.upper[3 * s + 1] = t.hi.y; f.upper[3 * s + 2] = t.hi.z;
+        f.first[s] = t.begin;
+        f.count[s] = t.left >= 0 ? 0 : t.count;
+        if (t.left >= 0) {
+            stack.push_back({t.left, int(s), it.depth + 1});
+            stack.push_back({t.right, int(s), it.depth + 1});
+        } else {
+            f.leaves.push_back(s);
+        }
+    }
+    // Escape index: the slot after the last slot of the subtree.
+    std::vector<uint32_t> subtree_end(count, 0);
+    for (size_t s = count; s-- > 0;) {
+        const TreeNode &t = tb.nodes[tree_of_slot[s]];
+        if (t.left < 0) subtree_end[s] = uint32_t(s + 1);
+        else {
+            const uint32_t l = slot[t.left], r = slot[t.right];
+            f.left_child[s] = l;
+            f.right_child[s] = r;
+            subtree_end[s] = std::max(subtree_end[l], subtree_end[r]);
+        }
+    }
+    for (size_t s = 0; s < count; ++s) f.escape[s] = subtree_end[s];
+}
+
+}  // namespace khs

@@ -148,6 +148,10 @@ class ContactRecord(ctypes.Structure):
                 ("reserved", c_u32), ("gap", c_f64)]
 
 
+class KernelTiming(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 40), ("launches", c_u64), ("total_milliseconds", c_f64)]
+
+
 CONTACT_DTYPE = np.dtype([("candidate_count", "<u4"), ("closest_triangle", "<u4"), ("active", "<u4"),
                           ("reserved", "<u4"), ("gap", "<f8")])
 
@@ -199,7 +203,17 @@ EXTENSION_FUNCTIONS = [
     ("khsxGetSubstepRecordCount", c_u32, [VP]),
     ("khsxCopySubstepRecords", ctypes.c_int, [VP, P(SubstepRecord), c_u32]),
     ("khsxCopyContactRecords", ctypes.c_int, [VP, VP, c_u32]),
+    ("khsxQueryContacts", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
+    ("khsxSetProfiling", ctypes.c_int, [VP, c_u32]),
+    ("khsxGetKernelTimings", c_u32, [VP, VP, c_u32]),
+    ("khsxResetKernelTimings", ctypes.c_int, [VP]),
+    ("khsxGetKernelLaunchCount", c_u64, [VP]),
+    ("khsxMeasurePipePeaks", ctypes.c_int, [P(c_f64), P(c_f64)]),
 ]
+
+# Entry points the CPU oracle does not provide (device-only measurement).
+DEVICE_ONLY = {"khsxSetProfiling", "khsxGetKernelTimings", "khsxResetKernelTimings", "khsxGetKernelLaunchCount",
+               "khsxMeasurePipePeaks"}
 
 
 def _vec3_buffer(values) -> np.ndarray:
@@ -220,6 +234,8 @@ class Library:
         # RTLD_LOCAL keeps two libraries exporting the same symbols apart.
         self.lib = ctypes.CDLL(str(self.path), mode=os.RTLD_LOCAL)
         for name, restype, argtypes in ABI_FUNCTIONS + (EXTENSION_FUNCTIONS if extensions else []):
+            if name in DEVICE_ONLY and not hasattr(self.lib, name):
+                continue
             fn = getattr(self.lib, name)
             fn.restype = restype
             fn.argtypes = argtypes
@@ -433,6 +449,28 @@ class HairSolver:
         records = (SubstepRecord * max(count, 1))()
         self._check(self._library.khsxCopySubstepRecords(self._handle, records, count))
         return list(records[:count])
+
+    def set_profiling(self, on: bool):
+        self._check(self._library.khsxSetProfiling(self._handle, 1 if on else 0))
+
+    def kernel_timings(self) -> dict:
+        cap = 64
+        buf = (KernelTiming * cap)()
+        n = int(self._library.khsxGetKernelTimings(self._handle, buf, cap))
+        return {buf[k].name.decode(): (int(buf[k].launches), float(buf[k].total_milliseconds)) for k in range(min(n, cap))}
+
+    def reset_kernel_timings(self):
+        self._check(self._library.khsxResetKernelTimings(self._handle))
+
+    def kernel_launches(self) -> int:
+        return int(self._library.khsxGetKernelLaunchCount(self._handle))
+
+    def query_contacts(self, q: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        count = self.build_stats().element_count
+        out = np.zeros(count, dtype=CONTACT_DTYPE)
+        self._check(self._library.khsxQueryContacts(self._handle, _ptr(q), q.size, _ptr(out), count))
+        return out
 
     def contact_records(self) -> np.ndarray:
         count = self.build_stats().element_count

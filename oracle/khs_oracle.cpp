@@ -64,6 +64,10 @@ constexpr int kBvhStack = 64;                        // cuda_backend.cu:26
 constexpr uint64_t kCheckpointMagic = 0x3154504348534bULL;  // cuda_backend.cu:27
 constexpr uint32_t kNone = 0xffffffffu;
 
+// Bounded-sample knob for CPU timing: when non-zero, a frame stops after
+// this many substeps (no adaptive retry).  Oracle-only; 0 = whole frames.
+static uint32_t g_substep_limit = 0;
+
 // ---------------------------------------------------------------------------
 // Geometry.
 
@@ -716,6 +720,37 @@ public:
         for (size_t e = 0; e < elements_.size(); ++e) out[e] = contact_records_.empty() ? KhsxContactRecord{0, kNone, 0, 0, 0.0} : contact_records_[e];
         return KHS_OK;
     }
+    // Contact classification of every element at positions q (the contact
+    // part of cuda_backend.cu:920-929 without energy).
+    KhsResult query_contacts(const double *q, uint64_t dof_count, KhsxContactRecord *out, uint32_t cap) const
+    {
+        if (!built_ || !q || dof_count < dof() || !out || cap < E()) return KHS_ERROR_INVALID_ARGUMENT;
+        const KhsHairMaterial &m = material_;
+        for (size_t ei = 0; ei < E(); ++ei) {
+            const Element &e = elements_[ei];
+            KhsxContactRecord r{0, kNone, 0, 0, std::numeric_limits<double>::infinity()};
+            if (has_collider() && !nodes_[e.i].fixed && e.contact) {
+                const V3 p0 = v3(q[6 * e.i], q[6 * e.i + 1], q[6 * e.i + 2]), p1 = v3(q[6 * e.j], q[6 * e.j + 1], q[6 * e.j + 2]);
+                Pair pair{1.0e300, 0.0, v3(1, 0, 0)};
+                uint32_t closest = kNone, cands = 0;
+                dev_bvh_.query(vmin(p0, p1), vmax(p0, p1), m.radius + m.collider_offset + m.barrier_distance, [&](uint32_t ti) {
+                    ++cands;
+                    const Tri &t = triangles_[ti];
+                    const Pair c = closest_segment_triangle_device(p0, p1, d_collider_current_[t.i0], d_collider_current_[t.i1], d_collider_current_[t.i2]);
+                    if (c.distance < pair.distance) { pair = c; closest = ti; }
+                });
+                r.candidate_count = cands;
+                if (closest != kNone) {
+                    r.closest_triangle = closest;
+                    r.gap = pair.distance - m.radius - m.collider_offset;
+                    r.active = (r.gap > desc_.minimum_gap && r.gap < m.barrier_distance) ? 1u : 0u;
+                }
+            }
+            out[ei] = r;
+        }
+        return KHS_OK;
+    }
+
     KhsResult build_stats(KhsBuildStats *s) const
     {
         if (!built_ || !s || s->struct_size < sizeof(KhsBuildStats)) return KHS_ERROR_INVALID_ARGUMENT;
@@ -1757,6 +1792,7 @@ private:
             bool crossed = false;
             KhsResult result = KHS_OK;
             for (uint32_t sub = 1; sub <= substeps; ++sub) {
+                if (g_substep_limit && sub > g_substep_limit) break;
                 progress_substep_.store(sub);
                 progress_iteration_.store(0);
                 KhsxSubstepRecord rec{};
@@ -2002,6 +2038,10 @@ KHS_API KhsResult khsxCopyState(const KhsSolver *s, double *q, double *v, uint64
 KHS_API uint32_t khsxGetSubstepRecordCount(const KhsSolver *s) { return s ? s->impl.record_count() : 0; }
 KHS_API KhsResult khsxCopySubstepRecords(const KhsSolver *s, KhsxSubstepRecord *r, uint32_t c) { return s ? s->impl.copy_records(r, c) : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API KhsResult khsxCopyContactRecords(const KhsSolver *s, KhsxContactRecord *r, uint32_t c) { return s ? s->impl.copy_contacts(r, c) : KHS_ERROR_INVALID_ARGUMENT; }
+KHS_API KhsResult khsxQueryContacts(KhsSolver *s, const double *q, uint64_t n, KhsxContactRecord *r, uint32_t c) { return s ? s->impl.query_contacts(q, n, r, c) : KHS_ERROR_INVALID_ARGUMENT; }
+
+// Oracle-only: stop every frame after n substeps (0 = whole frames).
+KHS_API void khsOracleSetSubstepLimit(uint32_t n) { khs_oracle::g_substep_limit = n; }
 
 // Oracle-only: thread count used by the OpenMP loops (0 = library default).
 KHS_API int khsOracleSetThreads(int n)

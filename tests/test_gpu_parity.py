@@ -1,0 +1,100 @@
+"""Parity of the GB300 plain FP64 solve with the CPU FP64 oracle.
+
+Same seeded scenes through both libraries; per frame:
+* node positions within 1e-6 m and rotation vectors within 1e-6 rad
+  (the tolerance stated for FP64 trajectories; the two differ only by the
+  rounding of transcendental functions and of reduction order),
+* identical Gauss-Newton / line-search / substep counts and identical
+  candidate and active-contact totals,
+* integer contact work bit-exact: at the GPU's own state the oracle's
+  broad + narrow phase gives the same per-element candidate count, closest
+  triangle, active flag and gap bits as the GPU's last evaluation, and on
+  identical perturbed states both libraries classify every element
+  identically.
+"""
+import numpy as np
+import pytest
+
+import parity
+import scenes
+import khs_native as kn
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+def _check(report, rotation_tol=None):
+    for k, fr in enumerate(report):
+        assert fr["result"][0] == fr["result"][1], (k, fr)
+        assert fr["max_position"] <= TOL, (k, fr)
+        assert fr["max_rotation"] <= (rotation_tol[k] if rotation_tol else TOL), (k, fr)
+        assert fr["newton"][0] == fr["newton"][1], (k, fr)
+        assert fr["line_search"][0] == fr["line_search"][1], (k, fr)
+        assert fr["substeps"][0] == fr["substeps"][1], (k, fr)
+        assert fr["candidates"][0] == fr["candidates"][1], (k, fr)
+        assert fr["active"][0] == fr["active"][1], (k, fr)
+        if "own_state_mismatch" in fr:
+            assert all(v == 0 for v in fr["own_state_mismatch"].values()), (k, fr)
+
+
+def test_sphere_static_single_frame(gpu_lib, oracle_lib):
+    sc = scenes.sphere_scene(motion=False, frames=1)
+    _check(parity.compare(parity.run(gpu_lib, sc, probe=oracle_lib), parity.run(oracle_lib, sc)))
+
+
+def test_sphere_moving(gpu_lib, oracle_lib):
+    sc = scenes.sphere_scene(motion=True, frames=3)
+    rep = parity.compare(parity.run(gpu_lib, sc, probe=oracle_lib), parity.run(oracle_lib, sc))
+    print(rep)
+    _check(rep)
+
+
+def _perturbed(scene, eps):
+    base = scene.root_points_at
+    scene.root_points_at = lambda f: base(f) * (1.0 + eps)
+    return scene
+
+
+def test_ellipsoid_contact(gpu_lib, oracle_lib):
+    """Contact-heavy frames that exhaust the 24-iteration Newton budget: the
+    weakly constrained twist of some nodes makes the rotation iterate
+    sensitive at the 1e-6 rad level to last-bit changes of the inputs.  The
+    oracle's own sensitivity is measured by rerunning it with the root
+    targets scaled by (1 + 1e-15); rotations must agree within
+    max(1e-6 rad, 4 x that sensitivity), positions within 1e-6 m."""
+    sc = scenes.ellipsoid_scene(strands=40, frames=2)
+    ref = parity.run(oracle_lib, sc)
+    rep = parity.compare(parity.run(gpu_lib, sc, probe=oracle_lib), ref)
+    own = parity.compare(parity.run(oracle_lib, _perturbed(scenes.ellipsoid_scene(strands=40, frames=2), 1e-15)), ref)
+    rot_tol = [max(TOL, 4.0 * fr["max_rotation"]) for fr in own]
+    print(rep, rot_tol)
+    _check(rep, rot_tol)
+
+
+def test_contact_query_bitexact_on_identical_states(gpu_lib, oracle_lib):
+    """Both libraries classify the same perturbed states identically."""
+    sc = scenes.ellipsoid_scene(strands=200, frames=1)
+    solvers = []
+    for lib in (gpu_lib, oracle_lib):
+        s = kn.HairSolver(lib)
+        scenes.load_into(s, sc)
+        solvers.append(s)
+    q0, _ = solvers[1].state()
+    rng = np.random.default_rng(7)
+    axes = np.array([0.09, 0.11, 0.12])
+    for trial in range(4):
+        q = q0.copy()
+        # Pull nodes towards the surface so many elements fall inside the
+        # barrier band, some inside the minimum gap.
+        x = q[:, :3]
+        r = np.linalg.norm(x / axes, axis=1, keepdims=True)
+        target = 1.0 + rng.uniform(-0.002, 0.01, size=r.shape)
+        q[:, :3] = x / r * target * np.where(rng.uniform(size=r.shape) < 0.5, 1.0, r / target)
+        a = solvers[0].query_contacts(q)
+        b = solvers[1].query_contacts(q)
+        mism = parity.records_equal(a, b)
+        assert all(v == 0 for v in mism.values()), (trial, mism)
+        assert a["active"].sum() > 0 and a["candidate_count"].sum() > 0
+    for s in solvers:
+        s.close()
