@@ -383,9 +383,13 @@ typedef enum KhsxSolveMode {
     /* Plain FP64 form: the reference method decision for decision, each
        stage a hand-written sm_103a kernel, FP64 throughout. */
     KHSX_MODE_PLAIN_FP64 = 0,
-    /* Mixed form: FP32 BVH bounds (outward rounded) and FP32 block LDL^T
-       with FP64 iterative refinement of the Gauss-Newton direction; FP64
-       kept for state, gradient, energies, barrier distances and CCD. */
+    /* Mixed form: FP32 broadphase (outward-rounded FP32 BVH boxes, exact
+       FP64 re-test at the leaves), FP32-filtered narrow phase and CCD /
+       sweep skip tests with exact FP64 decisions, exact early termination of
+       the CCD advancement.  State, gradient, Gauss-Newton blocks and their
+       factorisation, energies, barrier distances and CCD steps stay FP64:
+       an FP32 block factorisation does not converge under FP64 refinement
+       for these rods (tests/test_fp32_factorization_study.py). */
     KHSX_MODE_MIXED = 1
 } KhsxSolveMode;
 
@@ -407,7 +411,9 @@ typedef struct KhsxSubstepRecord {
     uint32_t newton_iterations;
     uint32_t line_search_evaluations;
     uint32_t steepest_fallbacks;
-    uint32_t refinement_sweeps;    /* mixed form: FP64 refinement sweeps */
+    uint32_t refinement_sweeps;    /* reserved (always 0, see KHSX_MODE_MIXED) */
+    uint32_t fp64_fallbacks;       /* reserved (always 0) */
+    uint32_t reserved;
     uint64_t contact_candidates;
     uint64_t active_contacts;
     double final_residual_norm;

@@ -400,6 +400,87 @@ KHS_HD ClosestPair closest_segment_triangle(V p0, V p1, V a, V b, V c)
     return out;
 }
 
+// ---- FP32 filters for the mixed form -----------------------------------
+//
+// Single-precision segment-triangle distance on coordinates taken relative
+// to a local origin (the segment start, subtracted in FP64).  Used only to
+// discard candidates that provably cannot be the closest one, with a
+// relative margin far above the FP32 rounding of these few operations; the
+// decision among the survivors is taken in FP64 with the exact code above.
+struct F3 {
+    float x, y, z;
+};
+KHS_HD F3 f3(float x, float y, float z) { F3 r; r.x = x; r.y = y; r.z = z; return r; }
+KHS_HD F3 fsub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+KHS_HD F3 fadd(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+KHS_HD F3 fmulv(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+KHS_HD float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+KHS_HD F3 to_local(V p, V origin) { return f3(float(p.x - origin.x), float(p.y - origin.y), float(p.z - origin.z)); }
+
+KHS_HD F3 closest_point_triangle_f(F3 p, F3 a, F3 b, F3 c)
+{
+    const F3 ab = fsub(b, a), ac = fsub(c, a), ap = fsub(p, a);
+    const float d1 = fdot(ab, ap), d2 = fdot(ac, ap);
+    if (d1 <= 0.f && d2 <= 0.f) return a;
+    const F3 bp = fsub(p, b);
+    const float d3 = fdot(ab, bp), d4 = fdot(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) return b;
+    const float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) return fadd(a, fmulv(ab, d1 / (d1 - d3)));
+    const F3 cp = fsub(p, c);
+    const float d5 = fdot(ab, cp), d6 = fdot(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) return c;
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) return fadd(a, fmulv(ac, d2 / (d2 - d6)));
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f)
+        return fadd(b, fmulv(fsub(c, b), (d4 - d3) / ((d4 - d3) + (d5 - d6))));
+    const float inv = 1.f / (va + vb + vc);
+    return fadd(fadd(a, fmulv(ab, vb * inv)), fmulv(ac, vc * inv));
+}
+
+KHS_HD float segment_segment_distance_f(F3 p1, F3 q1, F3 p2, F3 q2)
+{
+    const F3 d1 = fsub(q1, p1), d2 = fsub(q2, p2), r = fsub(p1, p2);
+    const float a = fdot(d1, d1), e = fdot(d2, d2), f = fdot(d2, r);
+    float s = 0.f, t = 0.f;
+    if (!(a <= 1e-20f && e <= 1e-20f)) {
+        if (a <= 1e-20f) t = fminf(1.f, fmaxf(0.f, f / e));
+        else {
+            const float c = fdot(d1, r);
+            if (e <= 1e-20f) s = fminf(1.f, fmaxf(0.f, -c / a));
+            else {
+                const float b = fdot(d1, d2), den = a * e - b * b;
+                if (den > 0.f) s = fminf(1.f, fmaxf(0.f, (b * f - c * e) / den));
+                t = (b * s + f) / e;
+                if (t < 0.f) { t = 0.f; s = fminf(1.f, fmaxf(0.f, -c / a)); }
+                else if (t > 1.f) { t = 1.f; s = fminf(1.f, fmaxf(0.f, (b - c) / a)); }
+            }
+        }
+    }
+    const F3 w = fsub(fadd(p1, fmulv(d1, s)), fadd(p2, fmulv(d2, t)));
+    return sqrtf(fdot(w, w));
+}
+
+// FP32 segment-triangle distance (local coordinates) and the absolute
+// margin that bounds its deviation from the FP64 distance.
+KHS_HD float segment_triangle_distance_f(F3 p0, F3 p1, F3 a, F3 b, F3 c, float &margin)
+{
+    F3 w = fsub(p0, closest_point_triangle_f(p0, a, b, c));
+    float dist = sqrtf(fdot(w, w));
+    w = fsub(p1, closest_point_triangle_f(p1, a, b, c));
+    dist = fminf(dist, sqrtf(fdot(w, w)));
+    dist = fminf(dist, segment_segment_distance_f(p0, p1, a, b));
+    dist = fminf(dist, segment_segment_distance_f(p0, p1, b, c));
+    dist = fminf(dist, segment_segment_distance_f(p0, p1, c, a));
+    const float scale = fmaxf(fmaxf(fabsf(p1.x), fmaxf(fabsf(p1.y), fabsf(p1.z))),
+                              fmaxf(fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))),
+                                    fmaxf(fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z))),
+                                          fmaxf(fabsf(c.x), fmaxf(fabsf(c.y), fabsf(c.z))))));
+    margin = 1.0e-4f * (scale + dist) + 1.0e-9f;
+    return dist;
+}
+
 KHS_HD bool boxes_overlap(V al, V au, V bl, V bu, double p)
 {
     return al.x <= bu.x + p && bl.x <= au.x + p && al.y <= bu.y + p && bl.y <= au.y + p && al.z <= bu.z + p &&

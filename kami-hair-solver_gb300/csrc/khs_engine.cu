@@ -112,6 +112,7 @@ struct View {
     const uint32_t *tri;
     double *col_cur, *col_old;
     double *blo, *bhi;
+    float *blo32, *bhi32;  // outward-rounded copies for the mixed form
     const uint32_t *besc, *bfirst, *bcount, *border, *bleaves;
     const int32_t *bparent;
     const uint32_t *bleft, *bright;
@@ -154,6 +155,45 @@ template<class F> __device__ void bvh_query(const View &d, V lo, V hi, double pa
         for (uint32_t k = first; k < first + cnt; ++k) f(d.border[k]);
         i = d.besc[i];
     }
+}
+
+// Mixed-form walk: internal nodes are tested on outward-rounded FP32 boxes
+// against the outward-rounded FP32 query box (a superset of the FP64 test,
+// and an FP64 overlap of a leaf implies FP64 overlap of every ancestor);
+// leaves passing the FP32 test are re-tested exactly in FP64.  The
+// candidates and their order are therefore exactly those of bvh_query.
+template<class F> __device__ void bvh_query_mixed(const View &d, V lo, V hi, double pad, F &&f)
+{
+    const float lx = __double2float_rd(lo.x), ly = __double2float_rd(lo.y), lz = __double2float_rd(lo.z);
+    const float hx = __double2float_ru(hi.x), hy = __double2float_ru(hi.y), hz = __double2float_ru(hi.z);
+    const float p = __double2float_ru(pad);
+    uint32_t i = 0;
+    while (i < d.B) {
+        const float *nl = d.blo32 + 3 * size_t(i), *nh = d.bhi32 + 3 * size_t(i);
+        const bool hit = lx <= __fadd_ru(nh[0], p) && nl[0] <= __fadd_ru(hx, p) && ly <= __fadd_ru(nh[1], p) &&
+                         nl[1] <= __fadd_ru(hy, p) && lz <= __fadd_ru(nh[2], p) && nl[2] <= __fadd_ru(hz, p);
+        if (!hit) { i = d.besc[i]; continue; }
+        const uint32_t cnt = d.bcount[i];
+        if (cnt == 0) { ++i; continue; }
+        if (dm::boxes_overlap(lo, hi, load3(d.blo + 3 * size_t(i)), load3(d.bhi + 3 * size_t(i)), pad)) {
+            const uint32_t first = d.bfirst[i];
+            for (uint32_t k = first; k < first + cnt; ++k) f(d.border[k]);
+        }
+        i = d.besc[i];
+    }
+}
+
+template<bool MIXED, class F> __device__ __forceinline__ void bvh_walk(const View &d, V lo, V hi, double pad, F &&f)
+{
+    if (MIXED) bvh_query_mixed(d, lo, hi, pad, f);
+    else bvh_query(d, lo, hi, pad, f);
+}
+
+__device__ __forceinline__ float candidate_distance_f(const View &d, uint32_t t, V origin, dm::F3 p0, dm::F3 p1, float &m)
+{
+    const dm::F3 a = dm::to_local(tri_vertex(d, t, 0), origin), b = dm::to_local(tri_vertex(d, t, 1), origin),
+                 c = dm::to_local(tri_vertex(d, t, 2), origin);
+    return dm::segment_triangle_distance_f(p0, p1, a, b, c, m);
 }
 
 // ---- per-substep set-up ---------------------------------------------------
@@ -210,6 +250,10 @@ __global__ void __launch_bounds__(kBlock) k_refit(View d, int swept)
     }
     store3(d.blo + 3 * size_t(node), lo);
     store3(d.bhi + 3 * size_t(node), hi);
+    d.blo32[3 * size_t(node)] = __double2float_rd(lo.x); d.blo32[3 * size_t(node) + 1] = __double2float_rd(lo.y);
+    d.blo32[3 * size_t(node) + 2] = __double2float_rd(lo.z);
+    d.bhi32[3 * size_t(node)] = __double2float_ru(hi.x); d.bhi32[3 * size_t(node) + 1] = __double2float_ru(hi.y);
+    d.bhi32[3 * size_t(node) + 2] = __double2float_ru(hi.z);
     for (;;) {
         const int32_t p = d.bparent[node];
         if (p < 0) return;
@@ -221,8 +265,15 @@ __global__ void __launch_bounds__(kBlock) k_refit(View d, int swept)
         const uint32_t l = d.bleft[p], r = d.bright[p];
         const V llo = dm::v(blo[3 * l], blo[3 * l + 1], blo[3 * l + 2]), rlo = dm::v(blo[3 * r], blo[3 * r + 1], blo[3 * r + 2]);
         const V lhi = dm::v(bhi[3 * l], bhi[3 * l + 1], bhi[3 * l + 2]), rhi = dm::v(bhi[3 * r], bhi[3 * r + 1], bhi[3 * r + 2]);
-        store3(d.blo + 3 * size_t(p), dm::vmin(llo, rlo));
-        store3(d.bhi + 3 * size_t(p), dm::vmax(lhi, rhi));
+        const V plo = dm::vmin(llo, rlo), phi = dm::vmax(lhi, rhi);
+        store3(d.blo + 3 * size_t(p), plo);
+        store3(d.bhi + 3 * size_t(p), phi);
+        // Rounding is monotone, so rounding the merged FP64 box equals the
+        // merge of the rounded children.
+        d.blo32[3 * size_t(p)] = __double2float_rd(plo.x); d.blo32[3 * size_t(p) + 1] = __double2float_rd(plo.y);
+        d.blo32[3 * size_t(p) + 2] = __double2float_rd(plo.z);
+        d.bhi32[3 * size_t(p)] = __double2float_ru(phi.x); d.bhi32[3 * size_t(p) + 1] = __double2float_ru(phi.y);
+        d.bhi32[3 * size_t(p) + 2] = __double2float_ru(phi.z);
         node = uint32_t(p);
     }
 }
@@ -230,13 +281,17 @@ __global__ void __launch_bounds__(kBlock) k_refit(View d, int swept)
 // Conservative advancement of each moving triangle against the stationary
 // hair at the start of the substep (cuda_backend.cu:975-987).  Returns the
 // first failing triangle of this element in traversal order.
-__device__ bool sweep_element(const View &d, uint32_t e, SweepRecord *rec)
+// Mixed form: a candidate whose FP32 lower-bound clearance already lets the
+// first advancement step reach alpha = 1 cannot fail and is skipped (the
+// 1e-6 relative slack dwarfs the FP64 rounding of that one step).
+template<bool MIXED> __device__ bool sweep_element(const View &d, uint32_t e, SweepRecord *rec)
 {
     const uint32_t i = d.ei[e], j = d.ej[e];
     const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
     const double target = d.radius + d.offset + d.min_gap;
+    const dm::F3 f0 = dm::f3(0.f, 0.f, 0.f), f1 = dm::to_local(p1, p0);
     bool failed = false;
-    bvh_query(d, dm::vmin(p0, p1), dm::vmax(p0, p1), target, [&](uint32_t t) {
+    bvh_walk<MIXED>(d, dm::vmin(p0, p1), dm::vmax(p0, p1), target, [&](uint32_t t) {
         if (failed) return;
         const V oa = load3(d.col_old + 3 * size_t(d.tri[3 * t])), ob = load3(d.col_old + 3 * size_t(d.tri[3 * t + 1])),
                 oc = load3(d.col_old + 3 * size_t(d.tri[3 * t + 2]));
@@ -244,6 +299,12 @@ __device__ bool sweep_element(const View &d, uint32_t e, SweepRecord *rec)
                 dc = dm::gsub(tri_vertex(d, t, 2), oc);
         const double speed = fmax(dm::gnorm(da), fmax(dm::gnorm(db), dm::gnorm(dc)));
         if (speed < 1e-30) return;
+        if (MIXED) {
+            float m;
+            const float df = dm::segment_triangle_distance_f(f0, f1, dm::to_local(oa, p0), dm::to_local(ob, p0),
+                                                              dm::to_local(oc, p0), m);
+            if (0.8 * (double(df) - double(m) - target) >= speed * (1.0 + 1e-6)) return;
+        }
         double alpha = 0.0;
         bool end = false;
         dm::ClosestPair pair;
@@ -270,12 +331,12 @@ __device__ bool sweep_element(const View &d, uint32_t e, SweepRecord *rec)
     return failed;
 }
 
-__global__ void __launch_bounds__(kBlock) k_sweep(View d)
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_sweep(View d)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
     if (d.fixed[d.ei[e]] || !d.econtact[e]) return;
-    if (sweep_element(d, e, nullptr)) atomicMin(&d.sc->sweep_fail, e);
+    if (sweep_element<MIXED>(d, e, nullptr)) atomicMin(&d.sc->sweep_fail, e);
 }
 
 // Publishes the lowest failing element of k_sweep (with its first failing
@@ -288,7 +349,7 @@ __global__ void k_sweep_record(View d)
     d.mail->sweep_fail = e;
     if (e == kNone) return;
     SweepRecord rec{};
-    sweep_element(d, e, &rec);
+    sweep_element<false>(d, e, &rec);
     *d.sweep = rec;
 }
 
@@ -379,14 +440,39 @@ __global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int 
 
 // Broad + narrow phase of one element: every candidate in traversal order,
 // the first strictly closest triangle kept (cuda_backend.cu:920-926).
+// Mixed form: a first pass bounds the FP64 minimum by FP32 distances with
+// margins; the second pass evaluates in FP64 only the candidates whose lower
+// bound does not exceed that bound, in the same order, so the result (and
+// the first-found tie-break) equals the all-FP64 search.
+template<bool MIXED>
 __device__ __forceinline__ uint32_t closest_triangle(const View &d, V xi, V xj, double pad, uint32_t &cand,
                                                      dm::ClosestPair &pair)
 {
     uint32_t closest = kNone;
     cand = 0;
     pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
-    bvh_query(d, dm::vmin(xi, xj), dm::vmax(xi, xj), pad, [&](uint32_t t) {
+    const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
+    if (!MIXED) {
+        bvh_query(d, lo, hi, pad, [&](uint32_t t) {
+            ++cand;
+            const dm::ClosestPair c = dm::closest_segment_triangle(xi, xj, tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2));
+            if (c.distance < pair.distance) { pair = c; closest = t; }
+        });
+        return closest;
+    }
+    const dm::F3 p0 = dm::f3(0.f, 0.f, 0.f), p1 = dm::to_local(xj, xi);
+    float bound = 3.0e38f;
+    bvh_query_mixed(d, lo, hi, pad, [&](uint32_t t) {
         ++cand;
+        float m;
+        const float df = candidate_distance_f(d, t, xi, p0, p1, m);
+        bound = fminf(bound, df + m);
+    });
+    if (cand == 0) return kNone;
+    bvh_query_mixed(d, lo, hi, pad, [&](uint32_t t) {
+        float m;
+        const float df = candidate_distance_f(d, t, xi, p0, p1, m);
+        if (df - m > bound) return;
         const dm::ClosestPair c = dm::closest_segment_triangle(xi, xj, tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2));
         if (c.distance < pair.distance) { pair = c; closest = t; }
     });
@@ -395,7 +481,7 @@ __device__ __forceinline__ uint32_t closest_triangle(const View &d, V xi, V xj, 
 
 // Contact classification of every element at a caller-provided state
 // (positions of q_probe); used to check the integer contact work.
-__global__ void __launch_bounds__(kBlock) k_contact_query(View d, const double *q)
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact_query(View d, const double *q)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
@@ -405,7 +491,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_query(View d, const double *
     double gap = 0.0;
     if (d.has_collider && !d.fixed[i] && d.econtact[e]) {
         dm::ClosestPair pair;
-        closest = closest_triangle(d, load3(q + 6 * size_t(i)), load3(q + 6 * size_t(j)), d.radius + d.offset + d.dhat, cand, pair);
+        closest = closest_triangle<MIXED>(d, load3(q + 6 * size_t(i)), load3(q + 6 * size_t(j)), d.radius + d.offset + d.dhat, cand, pair);
         if (closest != kNone) {
             flags |= kFlagClosest;
             gap = pair.distance - d.radius - d.offset;
@@ -421,7 +507,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_query(View d, const double *
 
 // Per element: elastic energy (+ gradient and GN blocks) and barrier contact
 // against the closest BVH candidate (cuda_backend.cu:899-939).
-__global__ void __launch_bounds__(kBlock) k_elem_eval(View d, int gradient)
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_elem_eval(View d, int gradient)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
@@ -460,7 +546,7 @@ __global__ void __launch_bounds__(kBlock) k_elem_eval(View d, int gradient)
     double gap = 0.0, ce = 0.0;
     if (d.has_collider && !fi && d.econtact[e]) {
         dm::ClosestPair pair;
-        closest = closest_triangle(d, xi, xj, d.radius + d.offset + d.dhat, cand, pair);
+        closest = closest_triangle<MIXED>(d, xi, xj, d.radius + d.offset + d.dhat, cand, pair);
         if (closest != kNone) {
             flags |= kFlagClosest;
             gap = pair.distance - d.radius - d.offset;
@@ -696,20 +782,35 @@ __global__ void __launch_bounds__(128) k_block_solve(View d)
     }
     uint32_t maxlen = len;
     for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(FULL, maxlen, o));
+    // The inputs of node t + 1 (its diagonal block row, gradient entry, the
+    // coupling block to t + 2 and the column of U_t) are loaded while node t
+    // is being eliminated, so the memory latency stays off the sequential
+    // chain along the strand.
+    double nd[6], nu[6], nuc[6], ng = 0.0;
+    auto fetch = [&](uint32_t t) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) nd[c] = on ? d.diag[36 * n + 6 * r + c] : 0.0;
+        ng = on ? d.grad[6 * n + r] : 0.0;
+        const bool up = on && t + 1 < len;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) nu[c] = up ? d.upper[36 * n + 6 * r + c] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) nuc[q] = (on && t > 0) ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
+    };
+    fetch(0);
     double Crow[6] = {0, 0, 0, 0, 0, 0}, dprev = 0.0;
     bool failed = false;
     for (uint32_t t = 0; t < maxlen; ++t) {
         const bool on = t < len && !failed;
         const size_t n = begin + t;
-        double a[6], inv[6], rhs = 0.0;
+        double a[6], inv[6], urow[6], ucol[6], rhs = -ng;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) { a[c] = on ? d.diag[36 * n + 6 * r + c] : 0.0; inv[c] = (c == r) ? 1.0 : 0.0; }
-        if (on) rhs = -d.grad[6 * n + r];
+        for (int c = 0; c < 6; ++c) { a[c] = nd[c]; inv[c] = (c == r) ? 1.0 : 0.0; ucol[c] = nuc[c]; urow[c] = nu[c]; }
+        if (t + 1 < maxlen) fetch(t + 1);
         if (t > 0) {
             // B -= U_{n-1}^T C_{n-1}, rhs -= U_{n-1}^T d'_{n-1}
-            double ucol[6];
-#pragma unroll
-            for (int q = 0; q < 6; ++q) ucol[q] = on ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
             double sum[6] = {0, 0, 0, 0, 0, 0}, sr = 0.0;
 #pragma unroll
             for (int q = 0; q < 6; ++q) {
@@ -721,39 +822,44 @@ __global__ void __launch_bounds__(128) k_block_solve(View d)
             for (int c = 0; c < 6; ++c) a[c] -= sum[c];
             rhs -= sr;
         }
-        // Relative diagonal shift.
+        // Relative diagonal shift max(1e-12 max|a_ii|, 1e-24).
         double diag_r = 0.0;
 #pragma unroll
         for (int c = 0; c < 6; ++c) if (c == r) diag_r = a[c];
-        double scale = 0.0;
+        // |x| of a double compares like its sign-cleared bit pattern, so the
+        // maxima below are integer operations.
+        unsigned long long smax = 0ull;
 #pragma unroll
-        for (int q = 0; q < 6; ++q) scale = fmax(scale, fabs(__shfl_sync(FULL, diag_r, base + q)));
-        const double shift = fmax(1.0e-12 * scale, 1.0e-24);
+        for (int q = 0; q < 6; ++q) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(__shfl_sync(FULL, diag_r, base + q)) & 0x7fffffffffffffffull;
+            smax = b > smax ? b : smax;
+        }
+        const double shift = fmax(1.0e-12 * __longlong_as_double((long long)smax), 1.0e-24);
 #pragma unroll
         for (int c = 0; c < 6; ++c) if (c == r) a[c] += shift;
-        // Gauss-Jordan with partial pivoting.
+        // Gauss-Jordan with partial pivoting (first largest |pivot|).
         bool ok = true;
 #pragma unroll
         for (int col = 0; col < 6; ++col) {
             double mine = 0.0;
 #pragma unroll
             for (int c = 0; c < 6; ++c) if (c == col) mine = a[c];
+            const unsigned long long mb = (unsigned long long)__double_as_longlong(mine) & 0x7fffffffffffffffull;
             int pivot = col;
-            double best = fabs(__shfl_sync(FULL, mine, base + col));
+            unsigned long long best = __shfl_sync(FULL, mb, base + col);
 #pragma unroll
             for (int row = col + 1; row < 6; ++row) {
-                const double vrow = fabs(__shfl_sync(FULL, mine, base + row));
+                const unsigned long long vrow = __shfl_sync(FULL, mb, base + row);
                 if (vrow > best) { best = vrow; pivot = row; }
             }
-            if (best < 1.0e-30 || !isfinite(best)) ok = false;
-            // Swap rows col and pivot.
+            // best < 1e-30 or not finite (exponent all ones) => failure.
+            if (best < 0x39b4484bfeebc2a0ull || best >= 0x7ff0000000000000ull) ok = false;
             const int partner = r == col ? pivot : (r == pivot ? col : r);
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
                 a[c] = __shfl_sync(FULL, a[c], base + partner);
                 inv[c] = __shfl_sync(FULL, inv[c], base + partner);
             }
-            // Normalise the pivot row and eliminate the column elsewhere.
             double pv = 0.0;
 #pragma unroll
             for (int c = 0; c < 6; ++c) if (c == col) pv = a[c];
@@ -780,15 +886,14 @@ __global__ void __launch_bounds__(128) k_block_solve(View d)
             if (r == 0) atomicExch(&d.sc->solve_failed, 1);
         }
         // C_n = B^-1 U_n (zero at the strand tip), d'_n = B^-1 rhs.
-        const bool last = t + 1 >= len;
+        // (row q of U_n lives in lane q of the group)
+        double csum[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            double sum = 0.0;
-            if (on && !last)
+        for (int q = 0; q < 6; ++q)
 #pragma unroll
-                for (int q = 0; q < 6; ++q) sum += inv[q] * d.upper[36 * n + 6 * q + c];
-            Crow[c] = sum;
-        }
+            for (int c = 0; c < 6; ++c) csum[c] += inv[q] * __shfl_sync(FULL, urow[c], base + q);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) Crow[c] = csum[c];
         double dn = 0.0;
 #pragma unroll
         for (int q = 0; q < 6; ++q) dn += inv[q] * __shfl_sync(FULL, rhs, base + q);
@@ -799,22 +904,36 @@ __global__ void __launch_bounds__(128) k_block_solve(View d)
             d.dprime[6 * n + r] = dn;
         }
     }
-    // Back substitution d_n = d'_n - C_n d_{n+1}.
+    // Back substitution d_n = d'_n - C_n d_{n+1}, with the next node's C row
+    // and d' prefetched.
     double next = 0.0;
+    double pc[6], pd = 0.0;
+    auto fetch_back = [&](uint32_t t) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        pd = on ? d.dprime[6 * n + r] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) pc[q] = on ? d.cprime[36 * n + 6 * r + q] : 0.0;
+    };
+    if (maxlen) fetch_back(maxlen - 1);
     for (uint32_t t = maxlen; t-- > 0;) {
         const bool on = t < len && !failed;
         const size_t n = begin + t;
-        double value = on ? d.dprime[6 * n + r] : 0.0;
+        double value = pd, crow[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) crow[q] = pc[q];
+        if (t > 0) fetch_back(t - 1);
         const bool coupled = on && t + 1 < len;
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             const double dq = __shfl_sync(FULL, next, base + q);  // every lane, every time: no divergent shuffles
-            if (coupled) value -= d.cprime[36 * n + 6 * r + q] * dq;
+            if (coupled) value -= crow[q] * dq;
         }
         if (on) d.dir[6 * n + r] = value;
         next = on ? value : 0.0;
     }
 }
+
 
 // Preconditioned steepest descent d = -P g, zero at fixed nodes
 // (cuda_backend.cu:632-638).
@@ -874,7 +993,7 @@ __global__ void __launch_bounds__(kBlock) k_final_dir(View d)
 // Line-search CCD bound (cuda_backend.cu:989-1000); the minimum over all
 // elements and candidates is taken with an unsigned atomicMin on the bit
 // pattern of the non-negative step.
-__global__ void __launch_bounds__(kBlock) k_ccd(View d)
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_ccd(View d)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
@@ -886,12 +1005,27 @@ __global__ void __launch_bounds__(kBlock) k_ccd(View d)
     const V hi = dm::vmax(dm::vmax(p0, p1), dm::vmax(p0 + d0, p1 + d1));
     const double target = d.radius + d.offset + d.min_gap;
     double local = 1.0;
-    bvh_query(d, lo, hi, target, [&](uint32_t t) {
+    const dm::F3 f0 = dm::f3(0.f, 0.f, 0.f), f1 = dm::to_local(p1, p0);
+    bvh_walk<MIXED>(d, lo, hi, target, [&](uint32_t t) {
         const double speed = fmax(dm::gnorm(d0), dm::gnorm(d1));
         if (speed < 1e-30) return;
         const V a = tri_vertex(d, t, 0), b = tri_vertex(d, t, 1), c = tri_vertex(d, t, 2);
+        if (MIXED) {
+            // Skip candidates whose first advancement step provably reaches 1.
+            float m;
+            const float df = dm::segment_triangle_distance_f(f0, f1, dm::to_local(a, p0), dm::to_local(b, p0),
+                                                              dm::to_local(c, p0), m);
+            if (0.8 * (double(df) - double(m) - target) >= speed * (1.0 + 1e-6)) return;
+        }
         double alpha = 0.0;
+        // Mixed form: every limit this candidate can still produce is
+        // >= 0.9 alpha (alpha only grows), so it stops as soon as that
+        // reaches the best limit known (its element's or the global one);
+        // the minimum is unchanged.
+        double bound = local;
+        if (MIXED) bound = fmin(bound, __longlong_as_double(*reinterpret_cast<volatile long long *>(&d.sc->ccd_bits)));
         for (int k = 0; k < 80; ++k) {
+            if (MIXED && 0.9 * alpha >= bound) return;
             const double dist = dm::closest_segment_triangle(dm::gadd(p0, dm::gmul(d0, alpha)), dm::gadd(p1, dm::gmul(d1, alpha)), a, b, c).distance;
             const double clear = dist - target;
             if (clear <= 0) { local = fmin(local, fmax(0.0, alpha * 0.9)); return; }
@@ -916,7 +1050,7 @@ __global__ void __launch_bounds__(kBlock) k_update_velocity(View d, double inv_d
 
 // Coulomb friction impulse (cuda_backend.cu:941-964); each element writes
 // its velocity change into its left/right node slots.
-__global__ void __launch_bounds__(kBlock) k_friction(View d, double dt)
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_friction(View d, double dt)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
@@ -927,7 +1061,7 @@ __global__ void __launch_bounds__(kBlock) k_friction(View d, double dt)
         const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
         uint32_t cand = 0;
         dm::ClosestPair pair;
-        const uint32_t closest = closest_triangle(d, p0, p1, d.radius + d.offset + d.dhat, cand, pair);
+        const uint32_t closest = closest_triangle<MIXED>(d, p0, p1, d.radius + d.offset + d.dhat, cand, pair);
         const double gap = pair.distance - d.radius - d.offset;
         if (closest != kNone && gap > 0.0 && gap < d.dhat) {
             const double w0 = 1.0 - pair.t, w1 = pair.t;
@@ -1128,6 +1262,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     bytes += 3 * padded<double>(E) + 2 * padded<uint32_t>(E) + padded<uint8_t>(E);
     bytes += 4 * padded<uint32_t>(S);
     bytes += padded<uint32_t>(3 * T) + 5 * padded<double>(3 * Vn);
+    bytes += 2 * padded<float>(3 * B);
     bytes += 2 * padded<double>(3 * B) + 4 * padded<uint32_t>(B) + padded<int32_t>(B) + 2 * padded<uint32_t>(B) +
              padded<uint32_t>(L) + padded<uint32_t>(T);
     bytes += padded<Partial>(kPartials) + padded<DirPartial>(kPartials) + padded<Scalars>(1);
@@ -1166,6 +1301,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.col_cur = a.take<double>(3 * Vn); v.col_old = a.take<double>(3 * Vn);
     I.col_frame_start = a.take<double>(3 * Vn); I.col_pending = a.take<double>(3 * Vn); I.col_a_copy = a.take<double>(3 * Vn);
     v.blo = a.take<double>(3 * B); v.bhi = a.take<double>(3 * B);
+    v.blo32 = a.take<float>(3 * B); v.bhi32 = a.take<float>(3 * B);
     uint32_t *besc = a.take<uint32_t>(B), *bfirst = a.take<uint32_t>(B), *bcount = a.take<uint32_t>(B);
     v.brefit = a.take<uint32_t>(B);
     int32_t *bparent = a.take<int32_t>(B);
@@ -1224,6 +1360,12 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     up(I.col_frame_start, hcol.data(), 3 * Vn * 8); up(I.col_pending, hcol.data(), 3 * Vn * 8);
     if (B) {
         up(v.blo, m.bvh.lower.data(), 3 * B * 8); up(v.bhi, m.bvh.upper.data(), 3 * B * 8);
+        std::vector<float> lo32(3 * B), hi32(3 * B);
+        for (size_t k = 0; k < 3 * B; ++k) {
+            lo32[k] = std::nextafter(float(m.bvh.lower[k]), -std::numeric_limits<float>::infinity());
+            hi32[k] = std::nextafter(float(m.bvh.upper[k]), std::numeric_limits<float>::infinity());
+        }
+        up(v.blo32, lo32.data(), 3 * B * 4); up(v.bhi32, hi32.data(), 3 * B * 4);
         up(besc, m.bvh.escape.data(), B * 4); up(bfirst, m.bvh.first.data(), B * 4); up(bcount, m.bvh.count.data(), B * 4);
         up(bparent, m.bvh.parent.data(), B * 4); up(bleft, m.bvh.left_child.data(), B * 4);
         up(bright, m.bvh.right_child.data(), B * 4); up(bleaves, m.bvh.leaves.data(), L * 4);
@@ -1404,7 +1546,8 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
     const bool trial = alpha >= 0.0;
     I.launch(gradient ? "k_node_eval_grad" : "k_node_eval_energy", k_node_eval, grid_for(v.N), kBlock, v, gradient ? 1 : 0,
              trial ? 1 : 0, trial ? alpha : 0.0, dt);
-    I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", k_elem_eval, grid_for(v.E), kBlock, v, gradient ? 1 : 0);
+    I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", mode_ ? k_elem_eval<true> : k_elem_eval<false>, grid_for(v.E),
+             kBlock, v, gradient ? 1 : 0);
     if (gradient) I.launch("k_node_sum", k_node_sum, grid_for(v.N), kBlock, v);
     I.launch("k_reduce_eval", k_reduce_eval, kPartials, kBlock, v, gradient ? 1 : 0);
     I.launch("k_final_eval", k_final_eval, 1, kBlock, v);
@@ -1437,9 +1580,10 @@ void Engine::make_steepest()
     limit_direction(I.mail_host->max_translation);
 }
 
-bool Engine::make_direction(KhsxSubstepRecord &rec)
+bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
 {
     Impl &I = *d_;
+    (void)grad_norm2;
     const unsigned warps = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
     I.launch("k_block_solve", k_block_solve, (warps + 3) / 4, 128, I.v);
     I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
@@ -1460,6 +1604,7 @@ bool Engine::make_direction(KhsxSubstepRecord &rec)
 KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
 {
     Impl &I = *d_;
+    last_dt_ = dt;
     const View &v = I.v;
     I.launch("k_precond", k_precond, grid_for(v.N), kBlock, v, dt);
     EvalStats current = evaluate(true, dt, -1.0);
@@ -1492,7 +1637,7 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
         }
         if (it == desc_.newton_iterations) break;
         progress_phase_.store(KHS_PHASE_LINEAR_SOLVE);
-        bool block_direction = make_direction(rec);
+        bool block_direction = make_direction(rec, current.grad_norm2);
         ++step_stats_.linear_solves;
         KHS_CUDA(cudaMemcpyAsync(v.q_base, v.q, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
         bool accepted = false;
@@ -1502,7 +1647,7 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
             I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, v);
             if (v.has_collider) {
                 progress_phase_.store(KHS_PHASE_CCD);
-                I.launch("k_ccd", k_ccd, grid_for(v.E), kBlock, v);
+                I.launch("k_ccd", mode_ ? k_ccd<true> : k_ccd<false>, grid_for(v.E), kBlock, v);
             }
             I.launch("k_final_dir", k_final_dir, 1, kBlock, v);
             I.check();
@@ -1617,7 +1762,7 @@ KhsResult Engine::run_frame(double frame_dt, const double *root_a, const double 
                 I.launch("k_collider_interp", k_collider_interp, grid_for(v.V), kBlock, v, I.col_a_copy, col_b, f);
                 I.launch("k_refit", k_refit, grid_for(v.L), kBlock, v, 1);
                 progress_phase_.store(KHS_PHASE_CCD);
-                I.launch("k_sweep", k_sweep, grid_for(v.E), kBlock, v);
+                I.launch("k_sweep", mode_ ? k_sweep<true> : k_sweep<false>, grid_for(v.E), kBlock, v);
                 I.launch("k_sweep_record", k_sweep_record, 1, 1, v);
                 I.check();
                 I.sync();
@@ -1651,7 +1796,7 @@ KhsResult Engine::run_frame(double frame_dt, const double *root_a, const double 
                 break;
             }
             if (v.has_collider && material_.friction > 0.0) {
-                I.launch("k_friction", k_friction, grid_for(v.E), kBlock, v, dt);
+                I.launch("k_friction", mode_ ? k_friction<true> : k_friction<false>, grid_for(v.E), kBlock, v, dt);
                 I.launch("k_friction_apply", k_friction_apply, grid_for(v.N), kBlock, v);
             }
             ++step_stats_.converged_substeps;
@@ -1806,7 +1951,8 @@ KhsResult Engine::query_contacts(const double *q, uint64_t dof, KhsxContactRecor
     Impl &I = *d_;
     if (!q || dof < 6 * uint64_t(I.v.N) || !out || capacity < I.v.E) return KHS_ERROR_INVALID_ARGUMENT;
     KHS_CUDA(cudaMemcpyAsync(I.v.q_base, q, 6 * size_t(I.v.N) * 8, cudaMemcpyHostToDevice, I.stream));
-    I.launch("k_contact_query", k_contact_query, grid_for(I.v.E), kBlock, I.v, I.v.q_base);
+    I.launch("k_contact_query", mode_ ? k_contact_query<true> : k_contact_query<false>, grid_for(I.v.E), kBlock, I.v,
+             I.v.q_base);
     KHS_CUDA(cudaGetLastError());
     return copy_contact_records(out, capacity);
 }

@@ -96,7 +96,7 @@ private:
                         uint32_t frame_count);
     KhsResult optimize_substep(double dt, KhsxSubstepRecord &rec);
     EvalStats evaluate(bool gradient, double dt, double alpha_for_trial);
-    bool make_direction(KhsxSubstepRecord &rec);
+    bool make_direction(KhsxSubstepRecord &rec, double grad_norm2);
     void make_steepest();
     void limit_direction(double max_translation);
 
@@ -106,7 +106,7 @@ private:
     bool initialized_ = false, animation_ready_ = false;
     uint32_t animation_frames_ = 0, current_frame_ = 0;
     std::vector<bool> root_frame_set_, collider_frame_set_;
-    double trust_radius_ = 0.0, max_rest_length_ = 0.0;
+    double trust_radius_ = 0.0, max_rest_length_ = 0.0, last_dt_ = 0.0;
     KhsStepStats step_stats_{};
     KhsGpuStats gpu_stats_{};
     KhsFailureDiagnostics failure_{};

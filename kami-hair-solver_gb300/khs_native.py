@@ -138,7 +138,7 @@ class SubstepRecord(ctypes.Structure):
     _fields_ = [
         ("struct_size", c_u32), ("substep", c_u32), ("newton_iterations", c_u32),
         ("line_search_evaluations", c_u32), ("steepest_fallbacks", c_u32), ("refinement_sweeps", c_u32),
-        ("contact_candidates", c_u64), ("active_contacts", c_u64), ("final_residual_norm", c_f64),
+        ("fp64_fallbacks", c_u32), ("reserved", c_u32), ("contact_candidates", c_u64), ("active_contacts", c_u64), ("final_residual_norm", c_f64),
         ("minimum_gap", c_f64),
     ]
 

@@ -799,6 +799,18 @@ public:
         cancel_.store(true);
         return KHS_OK;
     }
+    // Test hook: the Gauss-Newton system of the most recent gradient
+    // evaluation (FP64 blocks, gradient) and the strand layout.
+    void export_system(double *diag, double *upper, double *grad, uint32_t *strands) const
+    {
+        if (diag) std::copy(diag_.begin(), diag_.end(), diag);
+        if (upper) std::copy(upper_.begin(), upper_.end(), upper);
+        if (grad) std::copy(grad_.begin(), grad_.end(), grad);
+        if (strands)
+            for (size_t s = 0; s < strands_.size(); ++s) {
+                strands[3 * s] = strands_[s].first; strands[3 * s + 1] = strands_[s].count; strands[3 * s + 2] = strands_[s].fixed_count;
+            }
+    }
     uint32_t record_count() const { return uint32_t(records_.size()); }
     KhsResult copy_records(KhsxSubstepRecord *out, uint32_t cap) const
     {
@@ -2039,6 +2051,12 @@ KHS_API uint32_t khsxGetSubstepRecordCount(const KhsSolver *s) { return s ? s->i
 KHS_API KhsResult khsxCopySubstepRecords(const KhsSolver *s, KhsxSubstepRecord *r, uint32_t c) { return s ? s->impl.copy_records(r, c) : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API KhsResult khsxCopyContactRecords(const KhsSolver *s, KhsxContactRecord *r, uint32_t c) { return s ? s->impl.copy_contacts(r, c) : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API KhsResult khsxQueryContacts(KhsSolver *s, const double *q, uint64_t n, KhsxContactRecord *r, uint32_t c) { return s ? s->impl.query_contacts(q, n, r, c) : KHS_ERROR_INVALID_ARGUMENT; }
+
+// Oracle-only test hook (see Solver::export_system).
+KHS_API void khsOracleExportSystem(const KhsSolver *s, double *diag, double *upper, double *grad, uint32_t *strands)
+{
+    if (s) s->impl.export_system(diag, upper, grad, strands);
+}
 
 // Oracle-only: stop every frame after n substeps (0 = whole frames).
 KHS_API void khsOracleSetSubstepLimit(uint32_t n) { khs_oracle::g_substep_limit = n; }
