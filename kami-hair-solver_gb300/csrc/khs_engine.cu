@@ -64,7 +64,7 @@ struct Mailbox {
     double slope, dir_norm2, max_translation;
     unsigned long long ccd_bits;
     uint32_t sweep_fail;
-    uint32_t pad;
+    uint32_t pair_count;
 };
 
 // Atomic targets live in device memory; the publishing kernels copy them to
@@ -73,6 +73,8 @@ struct Scalars {
     unsigned long long ccd_bits;
     uint32_t sweep_fail;
     int solve_failed;
+    uint32_t pair_count;
+    uint32_t pad;
 };
 
 struct Partial {
@@ -111,8 +113,22 @@ struct View {
     const uint32_t *sfirst, *scount, *sfixed, *sorder;
     const uint32_t *tri;
     double *col_cur, *col_old;
+    float *col32;  // FP32 copy of col_cur for the mixed form's filters
     double *blo, *bhi;
     float *blo32, *bhi32;  // outward-rounded copies for the mixed form
+    // Mixed form: each BVH node packed in 32 bytes (FP32 outward-rounded box,
+    // escape index, leaf range), the per-element contact result of the
+    // separate contact pass, and the CCD (element, triangle) work list.
+    float4 *bnode;
+    double *c_t, *c_bary, *c_dist;
+    uint32_t *pair_elem, *pair_tri;
+    uint32_t pair_capacity;
+    // Per-substep leaf cache of the mixed contact pass: the leaves (DFS
+    // order) whose FP32 box overlaps the element box grown by kCacheSlack,
+    // and the element's node positions when they were collected.
+    uint32_t *cache_leaf;
+    uint8_t *cache_n;
+    double *cache_x;
     const uint32_t *besc, *bfirst, *bcount, *border, *bleaves;
     const int32_t *bparent;
     const uint32_t *bleft, *bright;
@@ -183,17 +199,137 @@ template<class F> __device__ void bvh_query_mixed(const View &d, V lo, V hi, dou
     }
 }
 
+// Exact FP64 leaf test of the reference (al <= bu + p && bl <= au + p per
+// axis) decided in FP32 when possible: if the query box rounded inwards
+// still overlaps the leaf box rounded inwards (one ulp inside the stored
+// outward box) with the padding rounded down, the FP64 test is true; if the
+// outward FP32 test failed it is false; only inside the rounding band is
+// the FP64 test evaluated.
+struct QueryBox {
+    V lo, hi;
+    double pad;
+    float olx, oly, olz, ohx, ohy, ohz, opad;  // outward-rounded box and padding
+    float ilx, ily, ilz, ihx, ihy, ihz, ipad;  // inward-rounded box and padding
+};
+
+__device__ __forceinline__ QueryBox make_query(V lo, V hi, double pad)
+{
+    QueryBox qb;
+    qb.lo = lo; qb.hi = hi; qb.pad = pad;
+    qb.olx = __double2float_rd(lo.x); qb.oly = __double2float_rd(lo.y); qb.olz = __double2float_rd(lo.z);
+    qb.ohx = __double2float_ru(hi.x); qb.ohy = __double2float_ru(hi.y); qb.ohz = __double2float_ru(hi.z);
+    qb.opad = __double2float_ru(pad);
+    qb.ilx = __double2float_ru(lo.x); qb.ily = __double2float_ru(lo.y); qb.ilz = __double2float_ru(lo.z);
+    qb.ihx = __double2float_rd(hi.x); qb.ihy = __double2float_rd(hi.y); qb.ihz = __double2float_rd(hi.z);
+    qb.ipad = __double2float_rd(pad);
+    return qb;
+}
+
+__device__ __forceinline__ bool maybe_overlap(const QueryBox &q, float4 a, float4 b)
+{
+    return q.olx <= __fadd_ru(b.x, q.opad) && a.x <= __fadd_ru(q.ohx, q.opad) && q.oly <= __fadd_ru(b.y, q.opad) &&
+           a.y <= __fadd_ru(q.ohy, q.opad) && q.olz <= __fadd_ru(b.z, q.opad) && a.z <= __fadd_ru(q.ohz, q.opad);
+}
+
+__device__ __forceinline__ bool leaf_overlap_exact(const View &d, uint32_t node, float4 a, float4 b, const QueryBox &q)
+{
+    const bool surely = q.ilx <= __fadd_rd(nextafterf(b.x, -INFINITY), q.ipad) &&
+                        nextafterf(a.x, INFINITY) <= __fadd_rd(q.ihx, q.ipad) &&
+                        q.ily <= __fadd_rd(nextafterf(b.y, -INFINITY), q.ipad) &&
+                        nextafterf(a.y, INFINITY) <= __fadd_rd(q.ihy, q.ipad) &&
+                        q.ilz <= __fadd_rd(nextafterf(b.z, -INFINITY), q.ipad) &&
+                        nextafterf(a.z, INFINITY) <= __fadd_rd(q.ihz, q.ipad);
+    if (surely) return true;
+    return dm::boxes_overlap(q.lo, q.hi, load3(d.blo + 3 * size_t(node)), load3(d.bhi + 3 * size_t(node)), q.pad);
+}
+
+// Same walk over the packed 32-byte nodes: one pair of 16-byte loads per
+// visited node (box + escape, box + leaf range (first << 4 | count)).
+template<class F> __device__ void bvh_query_packed(const View &d, V lo, V hi, double pad, F &&f)
+{
+    const QueryBox q = make_query(lo, hi, pad);
+    uint32_t i = 0;
+    while (i < d.B) {
+        const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
+        const uint32_t escape = __float_as_uint(a.w), leaf = __float_as_uint(b.w);
+        if (!maybe_overlap(q, a, b)) { i = escape; continue; }
+        if (leaf == 0) { ++i; continue; }
+        if (leaf_overlap_exact(d, i, a, b, q)) {
+            const uint32_t first = leaf >> 4, cnt = leaf & 15u;
+            for (uint32_t k = first; k < first + cnt; ++k) f(d.border[k]);
+        }
+        i = escape;
+    }
+}
+
+constexpr int kCacheLeaves = 16;
+constexpr double kCacheSlack = 1.0e-3;  // metres each node may move before the cache is bypassed
+constexpr uint8_t kCacheInvalid = 0xff;
+
+// Leaves whose FP32 outward box overlaps (lo, hi) padded by pad, in DFS
+// order, written to out (at most cap); returns the count, or cap + 1 on
+// overflow.
+__device__ uint32_t collect_leaves(const View &d, V lo, V hi, double pad, uint32_t *out, uint32_t cap)
+{
+    const QueryBox q = make_query(lo, hi, pad);
+    uint32_t i = 0, n = 0;
+    while (i < d.B) {
+        const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
+        const uint32_t escape = __float_as_uint(a.w), leaf = __float_as_uint(b.w);
+        if (!maybe_overlap(q, a, b)) { i = escape; continue; }
+        if (leaf == 0) { ++i; continue; }
+        if (n == cap) return cap + 1;
+        out[n++] = i;
+        i = escape;
+    }
+    return n;
+}
+
+// Candidate triangles of leaves given as a list (the cached leaves), with
+// the exact per-leaf test: the same triangles in the same order as
+// bvh_query, provided the list holds every leaf that test can accept.
+template<class F> __device__ void leaves_query(const View &d, const uint32_t *leaves, uint32_t n, V lo, V hi, double pad, F &&f)
+{
+    const QueryBox q = make_query(lo, hi, pad);
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t i = leaves[k];
+        const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
+        if (!maybe_overlap(q, a, b) || !leaf_overlap_exact(d, i, a, b, q)) continue;
+        const uint32_t leaf = __float_as_uint(b.w), first = leaf >> 4, cnt = leaf & 15u;
+        for (uint32_t t = first; t < first + cnt; ++t) f(d.border[t]);
+    }
+}
+
 template<bool MIXED, class F> __device__ __forceinline__ void bvh_walk(const View &d, V lo, V hi, double pad, F &&f)
 {
-    if (MIXED) bvh_query_mixed(d, lo, hi, pad, f);
+    if (MIXED) bvh_query_packed(d, lo, hi, pad, f);
     else bvh_query(d, lo, hi, pad, f);
 }
 
-__device__ __forceinline__ float candidate_distance_f(const View &d, uint32_t t, V origin, dm::F3 p0, dm::F3 p1, float &m)
+// FP32 distance of a candidate from the FP32 vertex copy, relative to an
+// FP32 origin (the segment start): no FP64 instruction.  Rounding the
+// vertices, the origin and the segment end to FP32 moves each coordinate by
+// at most 2^-24 of its magnitude, so the distance moves by at most
+// sqrt(3) * 2^-24 * (|vertex| + |origin| + |end|)_inf < 2.5e-7 * M, with M
+// bounding the absolute coordinates involved; that term is added to the
+// relative margin of the FP32 distance itself.
+__device__ __forceinline__ float candidate_distance_f(const View &d, uint32_t t, dm::F3 origin, dm::F3 p0, dm::F3 p1, float &m)
 {
-    const dm::F3 a = dm::to_local(tri_vertex(d, t, 0), origin), b = dm::to_local(tri_vertex(d, t, 1), origin),
-                 c = dm::to_local(tri_vertex(d, t, 2), origin);
-    return dm::segment_triangle_distance_f(p0, p1, a, b, c, m);
+    const float *c32 = d.col32;
+    const uint32_t i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
+    const float ax = c32[3 * i0], ay = c32[3 * i0 + 1], az = c32[3 * i0 + 2];
+    const float bx = c32[3 * i1], by = c32[3 * i1 + 1], bz = c32[3 * i1 + 2];
+    const float cx = c32[3 * i2], cy = c32[3 * i2 + 1], cz = c32[3 * i2 + 2];
+    const dm::F3 a = dm::f3(ax - origin.x, ay - origin.y, az - origin.z);
+    const dm::F3 b = dm::f3(bx - origin.x, by - origin.y, bz - origin.z);
+    const dm::F3 c = dm::f3(cx - origin.x, cy - origin.y, cz - origin.z);
+    const float df = dm::segment_triangle_distance_f(p0, p1, a, b, c, m);
+    const float vmax = fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fmaxf(fabsf(az), fabsf(bx))),
+                             fmaxf(fmaxf(fabsf(by), fabsf(bz)), fmaxf(fmaxf(fabsf(cx), fabsf(cy)), fabsf(cz))));
+    const float omax = fmaxf(fmaxf(fabsf(origin.x), fabsf(origin.y)), fabsf(origin.z));
+    const float emax = fmaxf(fmaxf(fabsf(p1.x), fabsf(p1.y)), fabsf(p1.z)) + omax;
+    m += 2.5e-7f * (vmax + omax + emax) + 1.0e-9f;
+    return df;
 }
 
 // ---- per-substep set-up ---------------------------------------------------
@@ -225,7 +361,9 @@ __global__ void __launch_bounds__(kBlock) k_collider_interp(View d, const double
     if (i >= d.V) return;
     const V cur = load3(d.col_cur + 3 * size_t(i));
     store3(d.col_old + 3 * size_t(i), cur);
-    store3(d.col_cur + 3 * size_t(i), dm::gadd(dm::gmul(load3(a + 3 * size_t(i)), 1.0 - f), dm::gmul(load3(b + 3 * size_t(i)), f)));
+    const V nv = dm::gadd(dm::gmul(load3(a + 3 * size_t(i)), 1.0 - f), dm::gmul(load3(b + 3 * size_t(i)), f));
+    store3(d.col_cur + 3 * size_t(i), nv);
+    d.col32[3 * size_t(i)] = float(nv.x); d.col32[3 * size_t(i) + 1] = float(nv.y); d.col32[3 * size_t(i) + 2] = float(nv.z);
 }
 
 // Bottom-up refit in one launch: each leaf thread computes its box and walks
@@ -254,6 +392,11 @@ __global__ void __launch_bounds__(kBlock) k_refit(View d, int swept)
     d.blo32[3 * size_t(node) + 2] = __double2float_rd(lo.z);
     d.bhi32[3 * size_t(node)] = __double2float_ru(hi.x); d.bhi32[3 * size_t(node) + 1] = __double2float_ru(hi.y);
     d.bhi32[3 * size_t(node) + 2] = __double2float_ru(hi.z);
+    if (d.bnode) {
+        float4 *pn = d.bnode + 2 * size_t(node);
+        pn[0].x = d.blo32[3 * size_t(node)]; pn[0].y = d.blo32[3 * size_t(node) + 1]; pn[0].z = d.blo32[3 * size_t(node) + 2];
+        pn[1].x = d.bhi32[3 * size_t(node)]; pn[1].y = d.bhi32[3 * size_t(node) + 1]; pn[1].z = d.bhi32[3 * size_t(node) + 2];
+    }
     for (;;) {
         const int32_t p = d.bparent[node];
         if (p < 0) return;
@@ -274,6 +417,11 @@ __global__ void __launch_bounds__(kBlock) k_refit(View d, int swept)
         d.blo32[3 * size_t(p) + 2] = __double2float_rd(plo.z);
         d.bhi32[3 * size_t(p)] = __double2float_ru(phi.x); d.bhi32[3 * size_t(p) + 1] = __double2float_ru(phi.y);
         d.bhi32[3 * size_t(p) + 2] = __double2float_ru(phi.z);
+        if (d.bnode) {
+            float4 *pn = d.bnode + 2 * size_t(p);
+            pn[0].x = d.blo32[3 * size_t(p)]; pn[0].y = d.blo32[3 * size_t(p) + 1]; pn[0].z = d.blo32[3 * size_t(p) + 2];
+            pn[1].x = d.bhi32[3 * size_t(p)]; pn[1].y = d.bhi32[3 * size_t(p) + 1]; pn[1].z = d.bhi32[3 * size_t(p) + 2];
+        }
         node = uint32_t(p);
     }
 }
@@ -438,6 +586,37 @@ __global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int 
     d.node_kinetic[n] = kin;
 }
 
+// Two-pass closest search of the mixed form over a candidate source
+// (source(fn) calls fn(triangle) for each candidate in traversal order):
+// FP32 distances with margins bound the FP64 minimum, then FP64 is evaluated
+// only for candidates whose lower bound does not exceed that bound.
+template<class Source>
+__device__ __forceinline__ uint32_t closest_triangle_in(const View &d, V xi, V xj, uint32_t &cand, dm::ClosestPair &pair,
+                                                        Source &&source)
+{
+    uint32_t closest = kNone;
+    cand = 0;
+    pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
+    const dm::F3 origin = dm::f3(float(xi.x), float(xi.y), float(xi.z));
+    const dm::F3 p0 = dm::f3(0.f, 0.f, 0.f), p1 = dm::f3(float(xj.x) - origin.x, float(xj.y) - origin.y, float(xj.z) - origin.z);
+    float bound = 3.0e38f;
+    source([&](uint32_t t) {
+        ++cand;
+        float m;
+        const float df = candidate_distance_f(d, t, origin, p0, p1, m);
+        bound = fminf(bound, df + m);
+    });
+    if (cand == 0) return kNone;
+    source([&](uint32_t t) {
+        float m;
+        const float df = candidate_distance_f(d, t, origin, p0, p1, m);
+        if (df - m > bound) return;
+        const dm::ClosestPair c = dm::closest_segment_triangle(xi, xj, tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2));
+        if (c.distance < pair.distance) { pair = c; closest = t; }
+    });
+    return closest;
+}
+
 // Broad + narrow phase of one element: every candidate in traversal order,
 // the first strictly closest triangle kept (cuda_backend.cu:920-926).
 // Mixed form: a first pass bounds the FP64 minimum by FP32 distances with
@@ -460,28 +639,16 @@ __device__ __forceinline__ uint32_t closest_triangle(const View &d, V xi, V xj, 
         });
         return closest;
     }
-    const dm::F3 p0 = dm::f3(0.f, 0.f, 0.f), p1 = dm::to_local(xj, xi);
-    float bound = 3.0e38f;
-    bvh_query_mixed(d, lo, hi, pad, [&](uint32_t t) {
-        ++cand;
-        float m;
-        const float df = candidate_distance_f(d, t, xi, p0, p1, m);
-        bound = fminf(bound, df + m);
-    });
-    if (cand == 0) return kNone;
-    bvh_query_mixed(d, lo, hi, pad, [&](uint32_t t) {
-        float m;
-        const float df = candidate_distance_f(d, t, xi, p0, p1, m);
-        if (df - m > bound) return;
-        const dm::ClosestPair c = dm::closest_segment_triangle(xi, xj, tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2));
-        if (c.distance < pair.distance) { pair = c; closest = t; }
-    });
-    return closest;
+    return closest_triangle_in(d, xi, xj, cand, pair, [&](auto &&fn) { bvh_query_packed(d, lo, hi, pad, fn); });
 }
 
 // Contact classification of every element at a caller-provided state
 // (positions of q_probe); used to check the integer contact work.
-template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact_query(View d, const double *q)
+// Contact classification of every element at the state q: candidate count,
+// closest triangle with its closest pair, gap and flags.  The mixed form runs
+// this as its own low-register pass before the element energy (and for the
+// contact-query entry point); the plain form searches inside k_elem_eval.
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact(View d, const double *q, int cache)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
@@ -489,9 +656,37 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact_query(V
     uint32_t cand = 0, closest = kNone;
     uint8_t flags = 0;
     double gap = 0.0;
+    dm::ClosestPair pair;
+    pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
     if (d.has_collider && !d.fixed[i] && d.econtact[e]) {
-        dm::ClosestPair pair;
-        closest = closest_triangle<MIXED>(d, load3(q + 6 * size_t(i)), load3(q + 6 * size_t(j)), d.radius + d.offset + d.dhat, cand, pair);
+        const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
+        const double pad = d.radius + d.offset + d.dhat;
+        if (MIXED && cache >= 0) {
+            uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
+            double *cx = d.cache_x + 6 * size_t(e);
+            if (cache == 1) {
+                // First evaluation after a refit: collect the leaves around
+                // the element box grown by the slack.
+                const V s3 = dm::v(kCacheSlack, kCacheSlack, kCacheSlack);
+                const uint32_t n = collect_leaves(d, dm::vmin(xi, xj) - s3, dm::vmax(xi, xj) + s3, pad, slots, kCacheLeaves);
+                d.cache_n[e] = n <= uint32_t(kCacheLeaves) ? uint8_t(n) : kCacheInvalid;
+                store3(cx, xi);
+                store3(cx + 3, xj);
+            }
+            const uint8_t n = d.cache_n[e];
+            const V ci = load3(cx), cj = load3(cx + 3);
+            const bool inside = n != kCacheInvalid && fabs(xi.x - ci.x) <= kCacheSlack && fabs(xi.y - ci.y) <= kCacheSlack &&
+                                fabs(xi.z - ci.z) <= kCacheSlack && fabs(xj.x - cj.x) <= kCacheSlack &&
+                                fabs(xj.y - cj.y) <= kCacheSlack && fabs(xj.z - cj.z) <= kCacheSlack;
+            if (inside) {
+                const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
+                closest = closest_triangle_in(d, xi, xj, cand, pair, [&](auto &&fn) { leaves_query(d, slots, n, lo, hi, pad, fn); });
+            } else {
+                closest = closest_triangle<MIXED>(d, xi, xj, pad, cand, pair);
+            }
+        } else {
+            closest = closest_triangle<MIXED>(d, xi, xj, pad, cand, pair);
+        }
         if (closest != kNone) {
             flags |= kFlagClosest;
             gap = pair.distance - d.radius - d.offset;
@@ -503,6 +698,9 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact_query(V
     d.c_tri[e] = closest;
     d.c_flags[e] = flags;
     d.c_gap[e] = gap;
+    d.c_t[e] = pair.t;
+    d.c_dist[e] = pair.distance;
+    store3(d.c_bary + 3 * size_t(e), pair.bary);
 }
 
 // Per element: elastic energy (+ gradient and GN blocks) and barrier contact
@@ -546,13 +744,21 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_elem_eval(View 
     double gap = 0.0, ce = 0.0;
     if (d.has_collider && !fi && d.econtact[e]) {
         dm::ClosestPair pair;
-        closest = closest_triangle<MIXED>(d, xi, xj, d.radius + d.offset + d.dhat, cand, pair);
+        if (MIXED) {
+            // Result of the contact pass at this same state.
+            cand = d.c_cand[e]; closest = d.c_tri[e]; flags = d.c_flags[e]; gap = d.c_gap[e];
+            pair.t = d.c_t[e]; pair.distance = d.c_dist[e]; pair.bary = load3(d.c_bary + 3 * size_t(e));
+        } else {
+            closest = closest_triangle<false>(d, xi, xj, d.radius + d.offset + d.dhat, cand, pair);
+            if (closest != kNone) {
+                flags |= kFlagClosest;
+                gap = pair.distance - d.radius - d.offset;
+                if (gap <= d.min_gap) flags |= kFlagInfeasible;
+                else if (gap < d.dhat) flags |= kFlagActive;
+            }
+        }
         if (closest != kNone) {
-            flags |= kFlagClosest;
-            gap = pair.distance - d.radius - d.offset;
-            if (gap <= d.min_gap) flags |= kFlagInfeasible;
-            else if (gap < d.dhat) {
-                flags |= kFlagActive;
+            if (flags & kFlagActive) {
                 const V a = tri_vertex(d, closest, 0), b = tri_vertex(d, closest, 1), c = tri_vertex(d, closest, 2);
                 const V bp = a * pair.bary.x + b * pair.bary.y + c * pair.bary.z;
                 double g0[3], g1[3];
@@ -985,8 +1191,10 @@ __global__ void __launch_bounds__(kBlock) k_final_dir(View d)
         d.mail->slope = gd; d.mail->dir_norm2 = dd; d.mail->max_translation = mx;
         d.mail->ccd_bits = d.sc->ccd_bits;
         d.mail->solve_failed = d.sc->solve_failed;
+        d.mail->pair_count = d.sc->pair_count;
         d.sc->ccd_bits = 0x3ff0000000000000ULL;  // 1.0
         d.sc->solve_failed = 0;
+        d.sc->pair_count = 0;
     }
 }
 
@@ -1039,6 +1247,67 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_ccd(View d)
     if (local < 1.0) atomicMin(&d.sc->ccd_bits, (unsigned long long)__double_as_longlong(local));
 }
 
+// Mixed-form CCD, load balanced: k_ccd_collect lists every (element,
+// triangle) candidate whose FP32 lower-bound clearance does not already let
+// the first advancement step reach alpha = 1; k_ccd_pairs runs the exact FP64
+// conservative advancement of cuda_backend.cu:989-1000 per listed pair and
+// stops a pair once 0.9 alpha reaches the global minimum found so far (every
+// limit the pair could still produce is >= 0.9 alpha).  The minimum equals
+// the per-element kernel's.
+__global__ void __launch_bounds__(kBlock) k_ccd_collect(View d)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    if (d.fixed[i] || !d.econtact[e]) return;
+    const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
+    const V d0 = load3(d.dir + 6 * size_t(i)), d1 = load3(d.dir + 6 * size_t(j));
+    const double speed = fmax(dm::gnorm(d0), dm::gnorm(d1));
+    if (speed < 1e-30) return;
+    const V lo = dm::vmin(dm::vmin(p0, p1), dm::vmin(p0 + d0, p1 + d1));
+    const V hi = dm::vmax(dm::vmax(p0, p1), dm::vmax(p0 + d0, p1 + d1));
+    const double target = d.radius + d.offset + d.min_gap;
+    const dm::F3 origin = dm::f3(float(p0.x), float(p0.y), float(p0.z));
+    const dm::F3 f0 = dm::f3(0.f, 0.f, 0.f), f1 = dm::f3(float(p1.x) - origin.x, float(p1.y) - origin.y, float(p1.z) - origin.z);
+    bvh_query_packed(d, lo, hi, target, [&](uint32_t t) {
+        float m;
+        const float df = candidate_distance_f(d, t, origin, f0, f1, m);
+        if (0.8 * (double(df) - double(m) - target) >= speed * (1.0 + 1e-6)) return;
+        const uint32_t slot = atomicAdd(&d.sc->pair_count, 1u);
+        if (slot < d.pair_capacity) { d.pair_elem[slot] = e; d.pair_tri[slot] = t; }
+    });
+}
+
+__global__ void __launch_bounds__(kBlock) k_ccd_pairs(View d)
+{
+    const uint32_t count = min(d.sc->pair_count, d.pair_capacity);
+    const double target = d.radius + d.offset + d.min_gap;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const uint32_t e = d.pair_elem[k], t = d.pair_tri[k];
+        const uint32_t i = d.ei[e], j = d.ej[e];
+        const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
+        const V d0 = load3(d.dir + 6 * size_t(i)), d1 = load3(d.dir + 6 * size_t(j));
+        const double speed = fmax(dm::gnorm(d0), dm::gnorm(d1));
+        const V a = tri_vertex(d, t, 0), b = tri_vertex(d, t, 1), c = tri_vertex(d, t, 2);
+        double limit = 2.0;  // no limit
+        double alpha = 0.0;
+        const double bound = __longlong_as_double(*reinterpret_cast<volatile long long *>(&d.sc->ccd_bits));
+        bool done = false;
+        for (int it = 0; it < 80 && !done; ++it) {
+            if (0.9 * alpha >= bound) { done = true; break; }
+            const double dist = dm::closest_segment_triangle(dm::gadd(p0, dm::gmul(d0, alpha)), dm::gadd(p1, dm::gmul(d1, alpha)), a, b, c).distance;
+            const double clear = dist - target;
+            if (clear <= 0) { limit = fmax(0.0, alpha * 0.9); done = true; break; }
+            const double advance = 0.8 * clear / speed;
+            if (alpha + advance >= 1) { done = true; break; }
+            if (advance < 1e-12) { limit = alpha; done = true; break; }
+            alpha += advance;
+        }
+        if (!done) limit = alpha;
+        if (limit < 1.0) atomicMin(&d.sc->ccd_bits, (unsigned long long)__double_as_longlong(limit));
+    }
+}
+
 // ---- end of substep -------------------------------------------------------
 
 __global__ void __launch_bounds__(kBlock) k_update_velocity(View d, double inv_dt)
@@ -1059,9 +1328,16 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_friction(View d
     const bool fi = d.fixed[i], fj = d.fixed[j];
     if (d.econtact[e] && !(fi && fj)) {
         const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
-        uint32_t cand = 0;
+        uint32_t cand = 0, closest;
         dm::ClosestPair pair;
-        const uint32_t closest = closest_triangle<MIXED>(d, p0, p1, d.radius + d.offset + d.dhat, cand, pair);
+        if (MIXED && !fi) {
+            // The last gradient evaluation ran the contact pass at this q and
+            // this collider state: reuse its closest pair.
+            closest = d.c_tri[e];
+            pair.t = d.c_t[e]; pair.distance = d.c_dist[e]; pair.bary = load3(d.c_bary + 3 * size_t(e));
+        } else {
+            closest = closest_triangle<MIXED>(d, p0, p1, d.radius + d.offset + d.dhat, cand, pair);
+        }
         const double gap = pair.distance - d.radius - d.offset;
         if (closest != kNone && gap > 0.0 && gap < d.dhat) {
             const double w0 = 1.0 - pair.t, w1 = pair.t;
@@ -1107,6 +1383,7 @@ __global__ void k_init_scalars(View d)
     d.sc->ccd_bits = 0x3ff0000000000000ULL;
     d.sc->sweep_fail = kNone;
     d.sc->solve_failed = 0;
+    d.sc->pair_count = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -1261,8 +1538,11 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     bytes += 3 * padded<uint32_t>(E) + padded<uint8_t>(E) + padded<double>(E) + 2 * padded<double>(3 * E);
     bytes += 3 * padded<double>(E) + 2 * padded<uint32_t>(E) + padded<uint8_t>(E);
     bytes += 4 * padded<uint32_t>(S);
-    bytes += padded<uint32_t>(3 * T) + 5 * padded<double>(3 * Vn);
-    bytes += 2 * padded<float>(3 * B);
+    bytes += padded<uint32_t>(3 * T) + 5 * padded<double>(3 * Vn) + padded<float>(3 * Vn);
+    bytes += 2 * padded<float>(3 * B) + padded<float4>(2 * B);
+    const size_t pair_capacity = std::min<size_t>(std::max<size_t>(size_t(1) << 20, 8 * E), size_t(16) << 20);
+    bytes += 2 * padded<double>(E) + padded<double>(3 * E) + 2 * padded<uint32_t>(pair_capacity);
+    bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E) + padded<double>(6 * E);
     bytes += 2 * padded<double>(3 * B) + 4 * padded<uint32_t>(B) + padded<int32_t>(B) + 2 * padded<uint32_t>(B) +
              padded<uint32_t>(L) + padded<uint32_t>(T);
     bytes += padded<Partial>(kPartials) + padded<DirPartial>(kPartials) + padded<Scalars>(1);
@@ -1299,9 +1579,16 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     uint32_t *sf = a.take<uint32_t>(S), *sc = a.take<uint32_t>(S), *sx = a.take<uint32_t>(S), *so = a.take<uint32_t>(S);
     uint32_t *tri = a.take<uint32_t>(3 * T);
     v.col_cur = a.take<double>(3 * Vn); v.col_old = a.take<double>(3 * Vn);
+    v.col32 = a.take<float>(3 * Vn);
     I.col_frame_start = a.take<double>(3 * Vn); I.col_pending = a.take<double>(3 * Vn); I.col_a_copy = a.take<double>(3 * Vn);
     v.blo = a.take<double>(3 * B); v.bhi = a.take<double>(3 * B);
     v.blo32 = a.take<float>(3 * B); v.bhi32 = a.take<float>(3 * B);
+    v.bnode = B ? a.take<float4>(2 * B) : nullptr;
+    v.c_t = a.take<double>(E); v.c_dist = a.take<double>(E); v.c_bary = a.take<double>(3 * E);
+    v.pair_elem = a.take<uint32_t>(pair_capacity); v.pair_tri = a.take<uint32_t>(pair_capacity);
+    v.pair_capacity = uint32_t(pair_capacity);
+    v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E); v.cache_x = a.take<double>(6 * E);
+    if (E) KHS_CUDA(cudaMemsetAsync(v.cache_n, kCacheInvalid, E, I.stream));
     uint32_t *besc = a.take<uint32_t>(B), *bfirst = a.take<uint32_t>(B), *bcount = a.take<uint32_t>(B);
     v.brefit = a.take<uint32_t>(B);
     int32_t *bparent = a.take<int32_t>(B);
@@ -1357,6 +1644,8 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     up(so, order.data(), S * 4);
     up(tri, m.tri.data(), 3 * T * 4);
     up(v.col_cur, hcol.data(), 3 * Vn * 8); up(v.col_old, hcol.data(), 3 * Vn * 8);
+    std::vector<float> hcol32(hcol.begin(), hcol.end());
+    up(v.col32, hcol32.data(), 3 * Vn * 4);
     up(I.col_frame_start, hcol.data(), 3 * Vn * 8); up(I.col_pending, hcol.data(), 3 * Vn * 8);
     if (B) {
         up(v.blo, m.bvh.lower.data(), 3 * B * 8); up(v.bhi, m.bvh.upper.data(), 3 * B * 8);
@@ -1366,6 +1655,17 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
             hi32[k] = std::nextafter(float(m.bvh.upper[k]), std::numeric_limits<float>::infinity());
         }
         up(v.blo32, lo32.data(), 3 * B * 4); up(v.bhi32, hi32.data(), 3 * B * 4);
+        std::vector<float4> packed(2 * B);
+        for (size_t k = 0; k < B; ++k) {
+            const uint32_t leaf = m.bvh.count[k] ? (m.bvh.first[k] << 4) | m.bvh.count[k] : 0u;
+            uint32_t esc = m.bvh.escape[k];
+            float e_f, l_f;
+            std::memcpy(&e_f, &esc, 4);
+            std::memcpy(&l_f, &leaf, 4);
+            packed[2 * k] = make_float4(lo32[3 * k], lo32[3 * k + 1], lo32[3 * k + 2], e_f);
+            packed[2 * k + 1] = make_float4(hi32[3 * k], hi32[3 * k + 1], hi32[3 * k + 2], l_f);
+        }
+        up(v.bnode, packed.data(), 2 * B * sizeof(float4));
         up(besc, m.bvh.escape.data(), B * 4); up(bfirst, m.bvh.first.data(), B * 4); up(bcount, m.bvh.count.data(), B * 4);
         up(bparent, m.bvh.parent.data(), B * 4); up(bleft, m.bvh.left_child.data(), B * 4);
         up(bright, m.bvh.right_child.data(), B * 4); up(bleaves, m.bvh.leaves.data(), L * 4);
@@ -1546,6 +1846,9 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
     const bool trial = alpha >= 0.0;
     I.launch(gradient ? "k_node_eval_grad" : "k_node_eval_energy", k_node_eval, grid_for(v.N), kBlock, v, gradient ? 1 : 0,
              trial ? 1 : 0, trial ? alpha : 0.0, dt);
+    if (mode_ && v.has_collider)
+        I.launch("k_contact", k_contact<true>, grid_for(v.E), kBlock, v, static_cast<const double *>(v.q), rebuild_cache_ ? 1 : 0);
+    rebuild_cache_ = false;
     I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", mode_ ? k_elem_eval<true> : k_elem_eval<false>, grid_for(v.E),
              kBlock, v, gradient ? 1 : 0);
     if (gradient) I.launch("k_node_sum", k_node_sum, grid_for(v.N), kBlock, v);
@@ -1647,11 +1950,23 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
             I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, v);
             if (v.has_collider) {
                 progress_phase_.store(KHS_PHASE_CCD);
-                I.launch("k_ccd", mode_ ? k_ccd<true> : k_ccd<false>, grid_for(v.E), kBlock, v);
+                if (mode_) {
+                    I.launch("k_ccd_collect", k_ccd_collect, grid_for(v.E), kBlock, v);
+                    I.launch("k_ccd_pairs", k_ccd_pairs, 152u * 8u, kBlock, v);
+                } else {
+                    I.launch("k_ccd", k_ccd<false>, grid_for(v.E), kBlock, v);
+                }
             }
             I.launch("k_final_dir", k_final_dir, 1, kBlock, v);
             I.check();
             I.sync();
+            if (mode_ && v.has_collider && I.mail_host->pair_count > v.pair_capacity) {
+                // Work list overflow: redo the bound with the per-element kernel.
+                I.launch("k_ccd", k_ccd<true>, grid_for(v.E), kBlock, v);
+                I.launch("k_final_dir", k_final_dir, 1, kBlock, v);
+                I.check();
+                I.sync();
+            }
             const double slope = I.mail_host->slope;
             alpha = 1.0;
             if (v.has_collider) {
@@ -1783,6 +2098,7 @@ KhsResult Engine::run_frame(double frame_dt, const double *root_a, const double 
                     break;
                 }
                 I.launch("k_refit", k_refit, grid_for(v.L), kBlock, v, 0);
+                rebuild_cache_ = true;
             }
             progress_phase_.store(KHS_PHASE_ASSEMBLING);
             result = optimize_substep(dt, rec);
@@ -1951,8 +2267,8 @@ KhsResult Engine::query_contacts(const double *q, uint64_t dof, KhsxContactRecor
     Impl &I = *d_;
     if (!q || dof < 6 * uint64_t(I.v.N) || !out || capacity < I.v.E) return KHS_ERROR_INVALID_ARGUMENT;
     KHS_CUDA(cudaMemcpyAsync(I.v.q_base, q, 6 * size_t(I.v.N) * 8, cudaMemcpyHostToDevice, I.stream));
-    I.launch("k_contact_query", mode_ ? k_contact_query<true> : k_contact_query<false>, grid_for(I.v.E), kBlock, I.v,
-             I.v.q_base);
+    I.launch("k_contact_query", mode_ ? k_contact<true> : k_contact<false>, grid_for(I.v.E), kBlock, I.v,
+             static_cast<const double *>(I.v.q_base), -1);
     KHS_CUDA(cudaGetLastError());
     return copy_contact_records(out, capacity);
 }

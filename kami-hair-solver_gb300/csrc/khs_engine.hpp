@@ -107,6 +107,7 @@ private:
     uint32_t animation_frames_ = 0, current_frame_ = 0;
     std::vector<bool> root_frame_set_, collider_frame_set_;
     double trust_radius_ = 0.0, max_rest_length_ = 0.0, last_dt_ = 0.0;
+    bool rebuild_cache_ = true;  // mixed form: recollect contact leaves at the next evaluation
     KhsStepStats step_stats_{};
     KhsGpuStats gpu_stats_{};
     KhsFailureDiagnostics failure_{};
