@@ -453,6 +453,33 @@ KHS_API KhsResult khsxQueryContacts(KhsSolver *solver, const double *q,
                                     KhsxContactRecord *records,
                                     uint32_t capacity);
 
+/* khsxQueryContacts for callers that cannot allocate memory while they run:
+   a render or audio thread with a fixed memory budget, a plug-in whose host
+   owns the device memory pool, or a process whose caching allocator already
+   holds the free device memory.  No counterpart in the reference.
+
+   Same arguments, results and solver-state guarantee as khsxQueryContacts,
+   but the call allocates nothing (no cudaMalloc, cudaFree, host heap or
+   library allocation): the caller's state and the records pass through one
+   file-scope device array of KHSX_NO_ALLOC_SCRATCH_BYTES per device, and
+   the solver's own contact records are left unchanged.
+   - Size limit: 48 bytes per internal node (rounded up to 256) plus 24
+     bytes per element must fit in KHSX_NO_ALLOC_SCRATCH_BYTES (about 100k
+     elements of 1000-strand scenes); larger solvers get
+     KHS_ERROR_INVALID_ARGUMENT.
+   - The first call on a device does set-up (it looks up the array's device
+     address and may load the device code); make it before any stream
+     capture.
+   - The array is shared by every solver on the device: calls that overlap
+     in time on one device race; serialise them.
+   - Errors are returned only (KHS_ERROR_INTERNAL for a CUDA failure); the
+     message of khsGetLastError is not updated. */
+#define KHSX_NO_ALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
+KHS_API KhsResult khsxQueryContactsNoAlloc(KhsSolver *solver, const double *q,
+                                           uint64_t dof_count,
+                                           KhsxContactRecord *records,
+                                           uint32_t capacity);
+
 /* ---- measurement ------------------------------------------------------- */
 
 /* With profiling on, every kernel launch of the solver is bracketed by CUDA

@@ -649,6 +649,14 @@ KHS_API KhsResult khsxQueryContacts(KhsSolver *s, const double *q, uint64_t dof_
     });
 }
 
+KHS_API KhsResult khsxQueryContactsNoAlloc(KhsSolver *s, const double *q, uint64_t dof_count,
+                                           KhsxContactRecord *records, uint32_t capacity)
+{
+    if (!s) return KHS_ERROR_INVALID_ARGUMENT;
+    if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+    return s->engine->query_contacts_no_alloc(q, dof_count, records, capacity);
+}
+
 KHS_API KhsResult khsxSetProfiling(KhsSolver *s, uint32_t enable)
 {
     return guarded(s, [&] {

@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <numeric>
 #include <stdexcept>
 
@@ -54,6 +55,8 @@ constexpr uint64_t kCheckpointMagic = 0x3154504348534bULL;  // same blob header 
 constexpr uint8_t kFlagActive = 1, kFlagInfeasible = 2, kFlagEnergy = 4, kFlagClosest = 8;
 
 inline unsigned grid_for(size_t n) { return unsigned((n + kBlock - 1) / kBlock); }
+// Every solver runs on device 0 (Engine::initialize selects it).
+constexpr int kDevice = 0;
 
 // Scalars produced by one evaluation / direction pass (host-mapped).
 struct Mailbox {
@@ -701,6 +704,45 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact(View d,
     d.c_t[e] = pair.t;
     d.c_dist[e] = pair.distance;
     store3(d.c_bary + 3 * size_t(e), pair.bary);
+}
+
+// ---- contact query without allocation -------------------------------------
+//
+// Scratch of khsxQueryContactsNoAlloc: the caller's state (48 bytes per
+// node) followed by the records (24 bytes per element), in a file-scope
+// device array of KHSX_NO_ALLOC_SCRATCH_BYTES.  One array per device and
+// process, shared by every solver on that device: calls that overlap in
+// time on one device race on it.
+__device__ __align__(256) unsigned char g_no_alloc_scratch[KHSX_NO_ALLOC_SCRATCH_BYTES];
+
+// k_contact without the leaf cache, writing the caller-facing record of each
+// element straight into the scratch instead of the solver's contact arrays
+// (the solver's own records are left as they are).  Every record below E is
+// written in full, so nothing in the scratch has to start at zero.
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact_query_records(View d, const double *q,
+                                                                                        KhsxContactRecord *out)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    uint32_t cand = 0, closest = kNone, active = 0;
+    double gap = __longlong_as_double(0x7ff0000000000000LL);  // +infinity
+    dm::ClosestPair pair;
+    if (d.has_collider && !d.fixed[i] && d.econtact[e]) {
+        const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
+        closest = closest_triangle<MIXED>(d, xi, xj, d.radius + d.offset + d.dhat, cand, pair);
+        if (closest != kNone) {
+            gap = pair.distance - d.radius - d.offset;
+            active = gap > d.min_gap && gap < d.dhat ? 1u : 0u;
+        }
+    }
+    KhsxContactRecord r;
+    r.candidate_count = cand;
+    r.closest_triangle = closest;
+    r.active = active;
+    r.reserved = 0;
+    r.gap = gap;
+    out[e] = r;
 }
 
 // Per element: elastic energy (+ gradient and GN blocks) and barrier contact
@@ -2271,6 +2313,62 @@ KhsResult Engine::query_contacts(const double *q, uint64_t dof, KhsxContactRecor
              static_cast<const double *>(I.v.q_base), -1);
     KHS_CUDA(cudaGetLastError());
     return copy_contact_records(out, capacity);
+}
+
+namespace {
+
+constexpr int kMaxScratchDevices = 64;
+std::mutex g_no_alloc_mutex;
+void *g_no_alloc_ptr[kMaxScratchDevices] = {};
+
+// Device address of g_no_alloc_scratch on device `device`, looked up once per
+// device with that device current (the first call may load the module).
+cudaError_t no_alloc_scratch(int device, void **ptr)
+{
+    if (device < 0 || device >= kMaxScratchDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_no_alloc_mutex);
+    if (!g_no_alloc_ptr[device]) {
+        int previous = 0;
+        cudaError_t err = cudaGetDevice(&previous);
+        if (err != cudaSuccess) return err;
+        if (previous != device && (err = cudaSetDevice(device)) != cudaSuccess) return err;
+        void *p = nullptr;
+        err = cudaGetSymbolAddress(&p, g_no_alloc_scratch);
+        if (previous != device) {
+            const cudaError_t back = cudaSetDevice(previous);
+            if (err == cudaSuccess) err = back;
+        }
+        if (err != cudaSuccess) return err;
+        if (!p) return cudaErrorInvalidSymbol;
+        g_no_alloc_ptr[device] = p;
+    }
+    *ptr = g_no_alloc_ptr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+KhsResult Engine::query_contacts_no_alloc(const double *q, uint64_t dof, KhsxContactRecord *out, uint32_t capacity)
+{
+    Impl &I = *d_;
+    const View &v = I.v;
+    if (!q || dof < 6 * uint64_t(v.N) || !out || capacity < v.E) return KHS_ERROR_INVALID_ARGUMENT;
+    const uint64_t q_bytes = 6 * uint64_t(v.N) * sizeof(double);
+    const uint64_t rec_offset = (q_bytes + 255) / 256 * 256;
+    if (rec_offset + uint64_t(v.E) * sizeof(KhsxContactRecord) > KHSX_NO_ALLOC_SCRATCH_BYTES) return KHS_ERROR_INVALID_ARGUMENT;
+    if (v.E == 0) return KHS_OK;
+    void *base = nullptr;
+    if (no_alloc_scratch(kDevice, &base) != cudaSuccess) return KHS_ERROR_INTERNAL;
+    double *q_dev = static_cast<double *>(base);
+    KhsxContactRecord *rec = reinterpret_cast<KhsxContactRecord *>(static_cast<unsigned char *>(base) + rec_offset);
+    if (cudaMemcpyAsync(q_dev, q, q_bytes, cudaMemcpyHostToDevice, I.stream) != cudaSuccess) return KHS_ERROR_INTERNAL;
+    if (mode_) k_contact_query_records<true><<<grid_for(v.E), kBlock, 0, I.stream>>>(v, q_dev, rec);
+    else k_contact_query_records<false><<<grid_for(v.E), kBlock, 0, I.stream>>>(v, q_dev, rec);
+    ++I.launches;
+    if (cudaGetLastError() != cudaSuccess) return KHS_ERROR_INTERNAL;
+    if (cudaMemcpyAsync(out, rec, size_t(v.E) * sizeof(KhsxContactRecord), cudaMemcpyDeviceToHost, I.stream) != cudaSuccess)
+        return KHS_ERROR_INTERNAL;
+    return cudaStreamSynchronize(I.stream) == cudaSuccess ? KHS_OK : KHS_ERROR_INTERNAL;
 }
 
 KhsResult Engine::copy_contact_records(KhsxContactRecord *out, uint32_t capacity) const

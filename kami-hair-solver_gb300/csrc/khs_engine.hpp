@@ -64,6 +64,9 @@ public:
     // Contact classification of every element at the given positions
     // (6 * N values) against the current collider.
     KhsResult query_contacts(const double *q, uint64_t dof, KhsxContactRecord *out, uint32_t capacity);
+    // The same query through a file-scope device scratch array: allocates
+    // nothing, leaves the solver's contact records alone, never throws.
+    KhsResult query_contacts_no_alloc(const double *q, uint64_t dof, KhsxContactRecord *out, uint32_t capacity);
 
     void set_mode(uint32_t mode) { mode_ = mode; }
     uint32_t mode() const { return mode_; }

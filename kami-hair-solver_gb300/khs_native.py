@@ -204,6 +204,7 @@ EXTENSION_FUNCTIONS = [
     ("khsxCopySubstepRecords", ctypes.c_int, [VP, P(SubstepRecord), c_u32]),
     ("khsxCopyContactRecords", ctypes.c_int, [VP, VP, c_u32]),
     ("khsxQueryContacts", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
+    ("khsxQueryContactsNoAlloc", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
     ("khsxSetProfiling", ctypes.c_int, [VP, c_u32]),
     ("khsxGetKernelTimings", c_u32, [VP, VP, c_u32]),
     ("khsxResetKernelTimings", ctypes.c_int, [VP]),
@@ -213,7 +214,11 @@ EXTENSION_FUNCTIONS = [
 
 # Entry points the CPU oracle does not provide (device-only measurement).
 DEVICE_ONLY = {"khsxSetProfiling", "khsxGetKernelTimings", "khsxResetKernelTimings", "khsxGetKernelLaunchCount",
-               "khsxMeasurePipePeaks"}
+               "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc"}
+
+# Size of the file-scope device scratch behind khsxQueryContactsNoAlloc
+# (KHSX_NO_ALLOC_SCRATCH_BYTES in the C header).
+NO_ALLOC_SCRATCH_BYTES = 8 * 1024 * 1024
 
 
 def _vec3_buffer(values) -> np.ndarray:
@@ -471,6 +476,14 @@ class HairSolver:
         out = np.zeros(count, dtype=CONTACT_DTYPE)
         self._check(self._library.khsxQueryContacts(self._handle, _ptr(q), q.size, _ptr(out), count))
         return out
+
+    def query_contacts_no_alloc(self, q: np.ndarray, out: np.ndarray) -> int:
+        """khsxQueryContactsNoAlloc into a caller-owned CONTACT_DTYPE array;
+        returns the raw result code (the entry point records no message)."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if out.dtype != CONTACT_DTYPE or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous CONTACT_DTYPE array")
+        return int(self._library.khsxQueryContactsNoAlloc(self._handle, _ptr(q), q.size, _ptr(out), out.size))
 
     def contact_records(self) -> np.ndarray:
         count = self.build_stats().element_count
