@@ -445,8 +445,8 @@ KHS_API KhsResult khsxCopyContactRecords(const KhsSolver *solver,
 
 /* Broad + narrow phase of every element at the caller's state q (6 values
    per internal node, as khsxCopyState returns) against the collider as
-   the last substep left it.  Does not change the solver state; records as
-   in khsxCopyContactRecords.  This is the integer contact work of one
+   the last substep left it.  Does not change q or v; the records (as in
+   khsxCopyContactRecords) replace those khsxCopyContactRecords returns.  This is the integer contact work of one
    evaluation, exposed so it can be compared bit for bit. */
 KHS_API KhsResult khsxQueryContacts(KhsSolver *solver, const double *q,
                                     uint64_t dof_count,
@@ -458,7 +458,7 @@ KHS_API KhsResult khsxQueryContacts(KhsSolver *solver, const double *q,
    owns the device memory pool, or a process whose caching allocator already
    holds the free device memory.  No counterpart in the reference.
 
-   Same arguments, results and solver-state guarantee as khsxQueryContacts,
+   Same arguments and results as khsxQueryContacts (q and v unchanged),
    but the call allocates nothing (no cudaMalloc, cudaFree, host heap or
    library allocation): the caller's state and the records pass through one
    file-scope device array of KHSX_NO_ALLOC_SCRATCH_BYTES per device, and
