@@ -8,12 +8,18 @@ A step is one animation frame (khsStepAnimationFrame) with every frame's
 root targets and collider vertices already resident in HBM; the metric is
 substeps per second.
 
-Prints ONE JSON line (rank 0).  Keys beyond the base contract:
-* roofline     -- the dominant kernel's FP64-pipe roofline: executed FP64
-                  flops per launch (per-element count measured once with ncu,
-                  see profiles/) / its CUDA-event duration measured live in
-                  the timed region, against the FMA-pipe peak measured by the
-                  library's probe on this GPU; traffic from the ncu capture.
+Prints ONE JSON line (rank 0).  ``value`` is the mixed form (FP32 filters,
+results identical to the plain form); the plain FP64 form is timed on the
+same frames and reported beside it as ``plain_fp64``.  Keys beyond the base
+contract:
+* roofline     -- the dominant kernel (largest share of device time in the
+                  timed region): algorithmic bytes per launch / its average
+                  CUDA-event duration measured live, against the measured HBM
+                  copy bandwidth; ``fp64`` adds algorithmic FP64 flops per
+                  launch against the FMA-pipe rate measured on this GPU by
+                  khsxMeasurePipePeaks (the heavy kernels are FP64-pipe
+                  bound).  ``traffic`` is DRAM bytes per launch from the ncu
+                  capture summarised under profiles/.
 * cpu_baseline -- the CPU oracle (a port of the reference method; the
                   reference has no CPU solver) on this host's cores, on a
                   bounded sample of the same workload.
@@ -55,11 +61,46 @@ import numpy as np  # noqa: E402
 METRIC = "substeps/s at 265k nodes, mixed+batched vs plain FP64 on 1 GB300 @≤1e-6 m; p99 latency"
 UNIT = "substeps/s"
 
-# Executed FP64 flops per element of the dominant kernel, measured once with
-# ncu (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}) on the body
-# scene; see profiles/.  None until measured.
-FP64_FLOPS_PER_ELEMENT = {"k_elem_eval_grad": None, "k_block_solve": None}
-DRAM_BYTES_PER_ELEMENT = {"k_elem_eval_grad": None, "k_block_solve": None}
+MEASURED_PEAKS = REPO / "MEASURED_PEAKS.json"
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# dominant kernels from one ncu capture of this workload; see profiles/.
+# k_contact was captured early in frame 5 (its traffic follows the contact
+# state); k_block_solve's does not depend on the state.
+NCU_TRAFFIC_BYTES: dict[str, float] = {"k_contact": 29.547776e6 + 5.12e3, "k_block_solve": 190.322688e6 + 67.055616e6}
+
+
+def algorithmic(name: str, nodes: int, free_nodes: int, elements: int, candidates: float):
+    """Algorithmic (bytes, FP64 flops) of one launch of kernel ``name``.
+
+    Bytes count every input read once and every output written once (FP64
+    SoA, the reference layout); flops count the reference method's
+    arithmetic, not this implementation's instructions:
+    * k_block_solve, per free node: read the diagonal and upper 6x6 blocks
+      and the gradient (288 + 288 + 48 B), write the direction (48 B); block
+      Thomas = B = D - U^T C (216 FMA), rhs (36), Gauss-Jordan inverse of a
+      6x6 with the identity appended (6 x (12 + 5 x 12) ops = 396 FMA-equiv),
+      C = B^-1 U (216), d' = B^-1 rhs (36), back substitution (36): 936 FMA
+      = 1872 flops.
+    * k_contact, per element: both node positions (48 B), node indices and
+      flags (10 B), the record written (candidates, triangle, flags, gap, t,
+      distance, barycentrics: 57 B); per candidate test 84 B (three vertices
+      and the index triple).
+    * k_elem_eval_grad, per element: q of both nodes (96 B), R and Jl of both
+      (288 B), constants (56 B), the two contributions (2 x (48 + 288) B) and
+      the upper block (288 B).
+    * k_node_eval_*, per node: q, q_old, v (144 B), constants (88 B),
+      gradient and diagonal written (48 + 48 B).
+    """
+    if name == "k_block_solve":
+        return 672.0 * free_nodes, 1872.0 * free_nodes
+    if name in ("k_contact", "k_contact_query"):
+        return 115.0 * elements + 84.0 * candidates, None
+    if name == "k_elem_eval_grad":
+        return 1400.0 * elements, None
+    if name.startswith("k_node_eval"):
+        return 328.0 * nodes, None
+    return None, None
 
 
 def _dist():
@@ -123,60 +164,70 @@ def _flush_l2(torch, buf):
     torch.cuda.synchronize()
 
 
-def cpu_oracle_sample(scene, substeps: int, threads: int | None = None) -> dict:
-    """Times the CPU oracle on the first ``substeps`` substeps of frame 1."""
+def _oracle_library():
     import khs_native as kn
-    import scenes
 
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle")], check=True)
     lib = kn.Library(REPO / "oracle" / "_build" / "libkhs_oracle.so")
     lib.lib.khsOracleSetThreads.restype = ctypes.c_int
-    cores = int(lib.lib.khsOracleSetThreads(ctypes.c_int(threads or os.cpu_count() or 1)))
-    lib.lib.khsOracleSetSubstepLimit(ctypes.c_uint32(substeps))
+    lib.lib.khsOracleSetThreads.argtypes = [ctypes.c_int]
+    lib.lib.khsOracleSetSubstepLimit.argtypes = [ctypes.c_uint32]
+    return lib
+
+
+def cpu_oracle_sample(scene, warm_frames: int, sample_frames: int, substeps: int, threads: int | None = None) -> dict:
+    """Times the CPU oracle on a bounded sample of the workload: frames
+    1..warm_frames run in full (untimed), then each of the next sample_frames
+    frames is cut after its first ``substeps`` substeps (timed)."""
+    import khs_native as kn
+    import scenes
+
+    lib = _oracle_library()
+    cores = int(lib.lib.khsOracleSetThreads(threads or os.cpu_count() or 1))
     s = kn.HairSolver(lib)
-    scenes.load_into(s, scene, frames=2)
-    t0 = time.perf_counter()
-    r = s._library.khsStepAnimationFrame(s.handle, 1, scene.frame_dt)
-    dt = time.perf_counter() - t0
+    scenes.load_into(s, scene, frames=warm_frames + sample_frames + 1)
+    lib.lib.khsOracleSetSubstepLimit(0)
+    for f in range(1, warm_frames + 1):
+        s._library.khsStepAnimationFrame(s.handle, f, scene.frame_dt)
+    lib.lib.khsOracleSetSubstepLimit(substeps)
+    done, newton, seconds, per_step = 0, 0, 0.0, []
+    for f in range(warm_frames + 1, warm_frames + sample_frames + 1):
+        t0 = time.perf_counter()
+        r = s._library.khsStepAnimationFrame(s.handle, f, scene.frame_dt)
+        dt = time.perf_counter() - t0
+        st = s.stats()
+        if r != kn.OK:
+            raise RuntimeError(f"oracle frame {f} failed ({r}): {s.last_error()}")
+        done += st.converged_substeps
+        newton += st.newton_iterations
+        seconds += dt
+        per_step.append(dt)
     s.close()
-    lib.lib.khsOracleSetSubstepLimit(ctypes.c_uint32(0))
-    return {"value": substeps / dt, "unit": UNIT, "cores": cores, "kind": "port", "result": int(r),
-            "sample": f"first {substeps} substep(s) of frame 1 of the same body scene, oracle on {cores} threads",
-            "seconds": dt}
+    lib.lib.khsOracleSetSubstepLimit(0)
+    return {"value": done / seconds, "unit": UNIT, "cores": cores, "kind": "port", "seconds": seconds,
+            "substeps": done, "newton_iterations": newton, "per_step_s": per_step,
+            "sample": f"first {substeps} substeps of frames {warm_frames + 1}-{warm_frames + sample_frames} of the same "
+                      f"body scene after frames 1-{warm_frames} in full (untimed); CPU FP64 oracle on {cores} threads"}
 
 
 def run_reference(args) -> None:
     world, rank = _dist()
     if rank != 0:
         return
-    import khs_native as kn
     import scenes
 
-    subprocess.run(["make", "-s", "-C", str(REPO / "oracle")], check=True)
-    lib = kn.Library(REPO / "oracle" / "_build" / "libkhs_oracle.so")
-    lib.lib.khsOracleSetThreads.restype = ctypes.c_int
-    cores = int(lib.lib.khsOracleSetThreads(ctypes.c_int(os.cpu_count() or 1)))
-    lib.lib.khsOracleSetSubstepLimit(ctypes.c_uint32(1))
     scene = scenes.body_scene(frames=args.warmup + args.steps + 1)
-    s = kn.HairSolver(lib)
-    scenes.load_into(s, scene)
-    for f in range(1, args.warmup + 1):
-        s._library.khsStepAnimationFrame(s.handle, f, scene.frame_dt)
-    t0 = time.perf_counter()
-    for f in range(args.warmup + 1, args.warmup + args.steps + 1):
-        s._library.khsStepAnimationFrame(s.handle, f, scene.frame_dt)
-    dt = time.perf_counter() - t0
-    s.close()
-    value = args.steps / dt
+    cpu = cpu_oracle_sample(scene, args.warmup, args.steps, args.cpu_substeps)
+    value = cpu["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded body scene)",
+        "warmup": args.warmup, "ms_per_step": 1e3 * cpu["seconds"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded body scene)",
         "config": _config(scene, "reference-cpu-oracle"),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "each step = first substep of one frame of the body scene (CPU FP64 oracle, "
-                                   "the reference method restated; the reference has no CPU solver)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+                         "sample": cpu["sample"] + " (the reference method restated; the reference has no CPU solver)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "substeps": cpu["substeps"], "newton_iterations": cpu["newton_iterations"],
     }
     print(json.dumps(line), flush=True)
 
@@ -188,6 +239,85 @@ def _config(scene, mode: str) -> dict:
             "collider_vertices": int(len(scene.vertices)), "collider_triangles": int(len(scene.triangles)),
             "substeps_base": int(scene.desc["substeps"]), "max_substeps": int(scene.desc["maximum_substeps"]),
             "mode": mode, "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
+
+
+def time_frames(lib, scene, mode: int, args, torch, flush, world: int) -> dict:
+    """Warm-up frames, then the timed frames of one solve mode (device time
+    of each frame from the library's CUDA events, per-kernel timings on)."""
+    import khs_native as kn
+    import scenes
+
+    frames = args.warmup + args.steps + 1
+    solver = kn.HairSolver(lib)
+    scenes.load_into(solver, scene)
+    solver.set_solve_mode(mode)
+    for f in range(1, args.warmup + 1):
+        solver.step_animation_frame(f, scene.frame_dt)
+    solver.set_profiling(True)
+    solver.reset_kernel_timings()
+    launches0 = solver.kernel_launches()
+    clocks = ClockSampler()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    frame_ms, substeps, newton, candidates = [], 0, 0, 0
+    wall0 = time.perf_counter()
+    for f in range(args.warmup + 1, frames):
+        _flush_l2(torch, flush)
+        r = solver._library.khsStepAnimationFrame(solver.handle, f, scene.frame_dt)
+        if r != kn.OK:
+            raise RuntimeError(f"frame {f} failed ({r}): {solver.last_error()}")
+        frame_ms.append(solver.gpu_stats().last_frame_milliseconds)
+        st = solver.stats()
+        substeps += st.substeps
+        newton += st.newton_iterations
+        candidates += st.contact_candidate_count
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clock_info = clocks.stop()
+    out = {"device_s": sum(frame_ms) / 1e3, "wall_s": wall, "substeps": substeps, "newton": newton,
+           "candidates": candidates, "frame_ms": frame_ms, "clocks": clock_info,
+           "launches": solver.kernel_launches() - launches0, "timings": solver.kernel_timings(),
+           "stats": solver.build_stats()}
+    solver.set_profiling(False)
+    solver.close()
+    return out
+
+
+def _max_over_ranks(torch, world: int, x: float) -> float:
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _roofline(run: dict, fp64_peak: float) -> dict:
+    timings = run["timings"]
+    total = sum(ms for _, ms in timings.values()) or 1.0
+    name, (count, ms) = max(timings.items(), key=lambda kv: kv[1][1]) if timings else ("none", (0, 0.0))
+    st = run["stats"]
+    nodes, elements = int(st.internal_node_count), int(st.element_count)
+    free_nodes = nodes - int(st.fixed_node_count)
+    grad_evals = timings.get("k_elem_eval_grad", (0, 0.0))[0] or 1
+    cand_per_eval = run["candidates"] / grad_evals
+    per_launch_s = (ms / max(count, 1)) / 1e3
+    alg_bytes, alg_flops = algorithmic(name, nodes, free_nodes, elements, cand_per_eval)
+    peaks = json.loads(MEASURED_PEAKS.read_text()) if MEASURED_PEAKS.exists() else {}
+    hbm_peak = peaks.get("hbm_gbs")
+    achieved = alg_bytes / per_launch_s / 1e9 if (alg_bytes and per_launch_s > 0) else None
+    roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak if (achieved and hbm_peak) else None,
+            "traffic": NCU_TRAFFIC_BYTES.get(name), "algorithmic_bytes_per_launch": alg_bytes,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else None,
+            "avg_launch_ms": ms / max(count, 1), "launches": count, "share": ms / total,
+            "kernel_shares": {k: round(v[1] / total, 4) for k, v in sorted(timings.items(), key=lambda kv: -kv[1][1])}}
+    if alg_flops:
+        tf = alg_flops / per_launch_s / 1e12
+        roof["fp64"] = {"achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": tf / fp64_peak,
+                        "algorithmic_flops_per_launch": alg_flops,
+                        "peak_source": "measured FP64 FMA-pipe rate of this GPU (khsxMeasurePipePeaks)"}
+    return roof
 
 
 def run_ours(args) -> None:
@@ -206,66 +336,28 @@ def run_ours(args) -> None:
     lib = kn.Library(lib_path)
     fp64_peak, fp32_peak = ctypes.c_double(), ctypes.c_double()
     lib.khsxMeasurePipePeaks(ctypes.byref(fp64_peak), ctypes.byref(fp32_peak))
-    mode = {"plain": kn.MODE_PLAIN_FP64, "mixed": kn.MODE_MIXED}[args.mode]
-    frames = args.warmup + args.steps + 1
-    scene = scenes.body_scene(frames=frames)
-    solver = kn.HairSolver(lib)
-    scenes.load_into(solver, scene)
-    solver.set_solve_mode(mode)
+    scene = scenes.body_scene(frames=args.warmup + args.steps + 1)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    for f in range(1, args.warmup + 1):
-        solver.step_animation_frame(f, scene.frame_dt)
-    solver.set_profiling(True)
-    solver.reset_kernel_timings()
-    launches0 = solver.kernel_launches()
-    clocks = ClockSampler()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    frame_ms, substeps, wall0 = [], 0, time.perf_counter()
-    for f in range(args.warmup + 1, frames):
-        _flush_l2(torch, flush)
-        r = solver._library.khsStepAnimationFrame(solver.handle, f, scene.frame_dt)
-        if r != kn.OK:
-            raise RuntimeError(f"frame {f} failed ({r}): {solver.last_error()}")
-        frame_ms.append(solver.gpu_stats().last_frame_milliseconds)
-        substeps += solver.stats().substeps
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
-    clock_info = clocks.stop()
-    launches = solver.kernel_launches() - launches0
-    timings = solver.kernel_timings()
-    solver.set_profiling(False)
-    device_s = sum(frame_ms) / 1e3
-    t = torch.tensor([device_s], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    device_s = float(t.item())
-    value = world * substeps / device_s
-    solver.close()
+    modes = {"plain": kn.MODE_PLAIN_FP64, "mixed": kn.MODE_MIXED}
+    main = time_frames(lib, scene, modes[args.mode], args, torch, flush, world)
+    device_s = _max_over_ranks(torch, world, main["device_s"])
+    value = world * main["substeps"] / device_s
+    plain = None
+    if args.mode == "mixed" and not args.skip_plain:
+        ref = time_frames(lib, scene, kn.MODE_PLAIN_FP64, args, torch, flush, world)
+        plain_s = _max_over_ranks(torch, world, ref["device_s"])
+        plain = {"value": world * ref["substeps"] / plain_s, "unit": UNIT, "ms_per_step": 1e3 * plain_s / args.steps,
+                 "substeps": ref["substeps"], "newton_iterations": ref["newton"], "speedup_of_mixed": None,
+                 "top_kernels": dict(list(_roofline(ref, fp64_peak.value)["kernel_shares"].items())[:4])}
+        plain["speedup_of_mixed"] = value / plain["value"]
+        plain["same_iterates"] = ref["substeps"] == main["substeps"] and ref["newton"] == main["newton"]
 
     # End to end through the public API with host buffers.
     e2e = run_e2e(lib, scene, args, torch) if not args.skip_e2e else None
-
-    # Roofline of the dominant kernel.
-    total = sum(ms for _, ms in timings.values()) or 1.0
-    top = max(timings.items(), key=lambda kv: kv[1][1]) if timings else ("none", (0, 0.0))
-    name, (count, ms) = top
-    E = 258351
-    per_launch_s = (ms / max(count, 1)) / 1e3
-    flops_el = FP64_FLOPS_PER_ELEMENT.get(name)
-    bytes_el = DRAM_BYTES_PER_ELEMENT.get(name)
-    achieved = (flops_el * E / per_launch_s / 1e12) if (flops_el and per_launch_s > 0) else None
-    roofline = {"bound": "fp64", "kernel": name, "achieved": achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
-                "frac": (achieved / fp64_peak.value) if achieved else None,
-                "traffic": (bytes_el * E) if bytes_el else None,
-                "peak_source": "measured FP64 FMA-pipe rate of this GPU (khsxMeasurePipePeaks)",
-                "avg_launch_ms": ms / max(count, 1), "launches": count, "share": ms / total,
-                "kernel_shares": {k: round(v[1] / total, 4) for k, v in sorted(timings.items(), key=lambda kv: -kv[1][1])}}
+    roofline = _roofline(main, fp64_peak.value)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        cpu = cpu_oracle_sample(scenes.body_scene(frames=2), substeps=args.cpu_substeps)
+        cpu = cpu_oracle_sample(scene, args.warmup, 1, args.cpu_substeps)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -273,7 +365,9 @@ def run_ours(args) -> None:
             "vs_baseline": None, "dtype": "f64" if args.mode == "plain" else "f64+f32",
             "data": "synthetic (seeded body scene, see kami-hair-solver_gb300/scenes.py)",
             "config": _config(scene, args.mode), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clock_info, "gpu_launches": int(launches), "wall_s": wall, "substeps": substeps,
+            "plain_fp64": plain, "clocks": main["clocks"], "gpu_launches": int(main["launches"]),
+            "wall_s": main["wall_s"], "substeps": main["substeps"], "newton_iterations": main["newton"],
+            "frame_ms": [round(x, 2) for x in main["frame_ms"]], "fp64_pipe_peak_tflops": fp64_peak.value,
             "fp32_pipe_peak_tflops": fp32_peak.value,
         }
         print(json.dumps(line), flush=True)
@@ -334,10 +428,12 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--mode", choices=["plain", "mixed"], default="plain")
+    ap.add_argument("--mode", choices=["plain", "mixed"], default="mixed")
+    ap.add_argument("--skip-plain", action="store_true", help="do not time the plain FP64 form beside the mixed one")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--cpu-substeps", type=int, default=1)
+    ap.add_argument("--cpu-substeps", type=int, default=2,
+                    help="substeps per sampled frame in the CPU oracle legs")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
