@@ -77,7 +77,7 @@ struct Scalars {
     uint32_t sweep_fail;
     int solve_failed;
     uint32_t pair_count;
-    uint32_t pad;
+    uint32_t surv_count;  // entries of the mixed contact pass's FP64 work list
 };
 
 struct Partial {
@@ -132,6 +132,15 @@ struct View {
     uint32_t *cache_leaf;
     uint8_t *cache_n;
     double *cache_x;
+    // Mixed contact pass in three launches: FP32 vertex records of every
+    // triangle in leaf order (a, b, c as three float4, the triangle index in
+    // the first .w), the survivors of the FP32 filter per element (at most
+    // kSurvivors, in traversal order), their FP64 closest pairs (distance,
+    // t, barycentrics) and the (element, slot) work list of the FP64 pass.
+    float4 *tri32;
+    uint32_t *surv_tri, *surv_list;
+    uint8_t *surv_n;
+    double *surv_res;
     const uint32_t *besc, *bfirst, *bcount, *border, *bleaves;
     const int32_t *bparent;
     const uint32_t *bleft, *bright;
@@ -248,7 +257,9 @@ __device__ __forceinline__ bool leaf_overlap_exact(const View &d, uint32_t node,
 
 // Same walk over the packed 32-byte nodes: one pair of 16-byte loads per
 // visited node (box + escape, box + leaf range (first << 4 | count)).
-template<class F> __device__ void bvh_query_packed(const View &d, V lo, V hi, double pad, F &&f)
+// f receives the position of each candidate in leaf order (index into
+// border and tri32).
+template<class F> __device__ void bvh_positions_packed(const View &d, V lo, V hi, double pad, F &&f)
 {
     const QueryBox q = make_query(lo, hi, pad);
     uint32_t i = 0;
@@ -259,10 +270,15 @@ template<class F> __device__ void bvh_query_packed(const View &d, V lo, V hi, do
         if (leaf == 0) { ++i; continue; }
         if (leaf_overlap_exact(d, i, a, b, q)) {
             const uint32_t first = leaf >> 4, cnt = leaf & 15u;
-            for (uint32_t k = first; k < first + cnt; ++k) f(d.border[k]);
+            for (uint32_t k = first; k < first + cnt; ++k) f(k);
         }
         i = escape;
     }
+}
+
+template<class F> __device__ void bvh_query_packed(const View &d, V lo, V hi, double pad, F &&f)
+{
+    bvh_positions_packed(d, lo, hi, pad, [&](uint32_t k) { f(d.border[k]); });
 }
 
 constexpr int kCacheLeaves = 16;
@@ -288,10 +304,12 @@ __device__ uint32_t collect_leaves(const View &d, V lo, V hi, double pad, uint32
     return n;
 }
 
-// Candidate triangles of leaves given as a list (the cached leaves), with
-// the exact per-leaf test: the same triangles in the same order as
-// bvh_query, provided the list holds every leaf that test can accept.
-template<class F> __device__ void leaves_query(const View &d, const uint32_t *leaves, uint32_t n, V lo, V hi, double pad, F &&f)
+// Candidates of leaves given as a list (the cached leaves), with the exact
+// per-leaf test: the same candidates in the same order as the full walk,
+// provided the list holds every leaf that test can accept.  f receives
+// leaf-order positions.
+template<class F> __device__ void leaves_positions(const View &d, const uint32_t *leaves, uint32_t n, V lo, V hi, double pad,
+                                                   F &&f)
 {
     const QueryBox q = make_query(lo, hi, pad);
     for (uint32_t k = 0; k < n; ++k) {
@@ -299,8 +317,13 @@ template<class F> __device__ void leaves_query(const View &d, const uint32_t *le
         const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
         if (!maybe_overlap(q, a, b) || !leaf_overlap_exact(d, i, a, b, q)) continue;
         const uint32_t leaf = __float_as_uint(b.w), first = leaf >> 4, cnt = leaf & 15u;
-        for (uint32_t t = first; t < first + cnt; ++t) f(d.border[t]);
+        for (uint32_t t = first; t < first + cnt; ++t) f(t);
     }
+}
+
+template<class F> __device__ void leaves_query(const View &d, const uint32_t *leaves, uint32_t n, V lo, V hi, double pad, F &&f)
+{
+    leaves_positions(d, leaves, n, lo, hi, pad, [&](uint32_t k) { f(d.border[k]); });
 }
 
 template<bool MIXED, class F> __device__ __forceinline__ void bvh_walk(const View &d, V lo, V hi, double pad, F &&f)
@@ -704,6 +727,211 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact(View d,
     d.c_t[e] = pair.t;
     d.c_dist[e] = pair.distance;
     store3(d.c_bary + 3 * size_t(e), pair.bary);
+}
+
+// ---- mixed contact pass in three launches ---------------------------------
+//
+// k_contact_filter (per element): candidate count and the FP32 filter over
+// the triangle records in leaf order; the survivors (every candidate whose
+// FP32 lower bound does not exceed the smallest FP32 upper bound, in
+// traversal order) go to per-element slots and to a compact work list.
+// k_contact_exact (per survivor): the FP64 closest pair, with every lane of
+// a warp on the same code path.  k_contact_select (per element): the first
+// strictly closest survivor in traversal order.  Candidates that are not
+// survivors are strictly farther in FP64 than the minimum, so the result,
+// tie-break included, equals k_contact's and the all-FP64 search.
+
+constexpr int kSurvivors = 8;
+constexpr uint8_t kSurvOverflow = 0xff;
+
+// FP32 vertex records of every triangle in leaf order; run whenever col_cur
+// changes (after k_collider_interp and at set-up).
+__global__ void __launch_bounds__(kBlock) k_tri32(View d)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.T) return;
+    const uint32_t t = d.border[p];
+    const V a = tri_vertex(d, t, 0), b = tri_vertex(d, t, 1), c = tri_vertex(d, t, 2);
+    d.tri32[3 * size_t(p)] = make_float4(float(a.x), float(a.y), float(a.z), __uint_as_float(t));
+    d.tri32[3 * size_t(p) + 1] = make_float4(float(b.x), float(b.y), float(b.z), 0.0f);
+    d.tri32[3 * size_t(p) + 2] = make_float4(float(c.x), float(c.y), float(c.z), 0.0f);
+}
+
+// candidate_distance_f on the record at leaf-order position p (one 48-byte
+// record instead of an index triple and three vertex reads).
+__device__ __forceinline__ float record_distance_f(const View &d, uint32_t p, dm::F3 origin, dm::F3 p0, dm::F3 p1, float &m,
+                                                   uint32_t &t)
+{
+    const float4 r0 = __ldg(d.tri32 + 3 * size_t(p)), r1 = __ldg(d.tri32 + 3 * size_t(p) + 1),
+                 r2 = __ldg(d.tri32 + 3 * size_t(p) + 2);
+    t = __float_as_uint(r0.w);
+    const dm::F3 a = dm::f3(r0.x - origin.x, r0.y - origin.y, r0.z - origin.z);
+    const dm::F3 b = dm::f3(r1.x - origin.x, r1.y - origin.y, r1.z - origin.z);
+    const dm::F3 c = dm::f3(r2.x - origin.x, r2.y - origin.y, r2.z - origin.z);
+    const float df = dm::segment_triangle_distance_f(p0, p1, a, b, c, m);
+    const float vmax = fmaxf(fmaxf(fmaxf(fabsf(r0.x), fabsf(r0.y)), fmaxf(fabsf(r0.z), fabsf(r1.x))),
+                             fmaxf(fmaxf(fabsf(r1.y), fabsf(r1.z)), fmaxf(fmaxf(fabsf(r2.x), fabsf(r2.y)), fabsf(r2.z))));
+    const float omax = fmaxf(fmaxf(fabsf(origin.x), fabsf(origin.y)), fabsf(origin.z));
+    const float emax = fmaxf(fmaxf(fabsf(p1.x), fabsf(p1.y)), fabsf(p1.z)) + omax;
+    m += 2.5e-7f * (vmax + omax + emax) + 1.0e-9f;
+    return df;
+}
+
+// Filter of one element over a position source; returns the survivor count
+// (kSurvivors + 1 or more on overflow; the first kSurvivors are stored).
+template<class Source>
+__device__ __forceinline__ uint32_t filter_survivors(const View &d, uint32_t e, V xi, V xj, uint32_t &cand, Source &&source)
+{
+    const dm::F3 origin = dm::f3(float(xi.x), float(xi.y), float(xi.z));
+    const dm::F3 p0 = dm::f3(0.f, 0.f, 0.f), p1 = dm::f3(float(xj.x) - origin.x, float(xj.y) - origin.y, float(xj.z) - origin.z);
+    float bound = 3.0e38f;
+    cand = 0;
+    source([&](uint32_t p) {
+        ++cand;
+        float m;
+        uint32_t t;
+        const float df = record_distance_f(d, p, origin, p0, p1, m, t);
+        bound = fminf(bound, df + m);
+    });
+    if (cand == 0) return 0;
+    uint32_t n = 0;
+    uint32_t *slots = d.surv_tri + size_t(kSurvivors) * e;
+    source([&](uint32_t p) {
+        float m;
+        uint32_t t;
+        const float df = record_distance_f(d, p, origin, p0, p1, m, t);
+        if (df - m > bound) return;
+        if (n < uint32_t(kSurvivors)) slots[n] = t;
+        ++n;
+    });
+    return n;
+}
+
+__device__ __forceinline__ void write_contact(const View &d, uint32_t e, uint32_t closest, const dm::ClosestPair &pair)
+{
+    uint8_t flags = 0;
+    double gap = 0.0;
+    if (closest != kNone) {
+        flags |= kFlagClosest;
+        gap = pair.distance - d.radius - d.offset;
+        if (gap <= d.min_gap) flags |= kFlagInfeasible;
+        else if (gap < d.dhat) flags |= kFlagActive;
+    }
+    d.c_tri[e] = closest;
+    d.c_flags[e] = flags;
+    d.c_gap[e] = gap;
+    d.c_t[e] = pair.t;
+    d.c_dist[e] = pair.distance;
+    store3(d.c_bary + 3 * size_t(e), pair.bary);
+}
+
+__global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double *q, int cache)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = e < d.E;
+    uint32_t append = 0;
+    if (live) {
+        const uint32_t i = d.ei[e], j = d.ej[e];
+        uint32_t cand = 0, n = 0;
+        V xi = dm::v(0, 0, 0), xj = xi;
+        const bool enabled = d.has_collider && !d.fixed[i] && d.econtact[e];
+        bool inside = false;
+        uint8_t nl = 0;
+        const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
+        const double pad = d.radius + d.offset + d.dhat;
+        if (enabled) {
+            xi = load3(q + 6 * size_t(i)); xj = load3(q + 6 * size_t(j));
+            if (cache >= 0) {
+                double *cx = d.cache_x + 6 * size_t(e);
+                if (cache == 1) {
+                    const V s3 = dm::v(kCacheSlack, kCacheSlack, kCacheSlack);
+                    uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
+                    const uint32_t c = collect_leaves(d, dm::vmin(xi, xj) - s3, dm::vmax(xi, xj) + s3, pad, slots, kCacheLeaves);
+                    d.cache_n[e] = c <= uint32_t(kCacheLeaves) ? uint8_t(c) : kCacheInvalid;
+                    store3(cx, xi);
+                    store3(cx + 3, xj);
+                }
+                nl = d.cache_n[e];
+                const V ci = load3(cx), cj = load3(cx + 3);
+                inside = nl != kCacheInvalid && fabs(xi.x - ci.x) <= kCacheSlack && fabs(xi.y - ci.y) <= kCacheSlack &&
+                         fabs(xi.z - ci.z) <= kCacheSlack && fabs(xj.x - cj.x) <= kCacheSlack &&
+                         fabs(xj.y - cj.y) <= kCacheSlack && fabs(xj.z - cj.z) <= kCacheSlack;
+            }
+            const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
+            if (inside)
+                n = filter_survivors(d, e, xi, xj, cand, [&](auto &&fn) { leaves_positions(d, leaves, nl, lo, hi, pad, fn); });
+            else
+                n = filter_survivors(d, e, xi, xj, cand, [&](auto &&fn) { bvh_positions_packed(d, lo, hi, pad, fn); });
+        }
+        d.c_cand[e] = cand;
+        if (n > uint32_t(kSurvivors)) {
+            // Rare: more near-equal candidates than slots; finish in place.
+            uint32_t c2 = 0;
+            dm::ClosestPair pair;
+            const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
+            const uint32_t closest =
+                inside ? closest_triangle_in(d, xi, xj, c2, pair, [&](auto &&fn) { leaves_query(d, leaves, nl, lo, hi, pad, fn); })
+                       : closest_triangle<true>(d, xi, xj, pad, c2, pair);
+            write_contact(d, e, closest, pair);
+            d.surv_n[e] = kSurvOverflow;
+        } else {
+            d.surv_n[e] = uint8_t(n);
+            append = n;
+            if (n == 0) {
+                dm::ClosestPair pair;
+                pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
+                write_contact(d, e, kNone, pair);
+            }
+        }
+    }
+    // Warp-aggregated append of (element, slot) entries to the work list.
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint32_t incl = append;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(&d.sc->surv_count, total);
+    base = __shfl_sync(FULL, base, 31);
+    const uint32_t start = base + incl - append;
+    for (uint32_t k = 0; k < append; ++k) d.surv_list[start + k] = uint32_t(kSurvivors) * e + k;
+}
+
+__global__ void __launch_bounds__(kBlock) k_contact_exact(View d, const double *q)
+{
+    const uint32_t count = d.sc->surv_count;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const uint32_t slot = d.surv_list[k], e = slot / uint32_t(kSurvivors), t = d.surv_tri[slot];
+        const uint32_t i = d.ei[e], j = d.ej[e];
+        const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
+        const dm::ClosestPair c = dm::closest_segment_triangle(xi, xj, tri_vertex(d, t, 0), tri_vertex(d, t, 1), tri_vertex(d, t, 2));
+        double *r = d.surv_res + 5 * size_t(slot);
+        r[0] = c.distance; r[1] = c.t; r[2] = c.bary.x; r[3] = c.bary.y; r[4] = c.bary.z;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_contact_select(View d)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e == 0) d.sc->surv_count = 0;  // k_contact_exact, its only reader, has completed
+    if (e >= d.E) return;
+    const uint32_t n = d.surv_n[e];
+    if (n == 0 || n == kSurvOverflow) return;
+    uint32_t best = 0;
+    double bd = 1.0e300;
+    for (uint32_t k = 0; k < n; ++k) {
+        const double dist = d.surv_res[5 * (size_t(kSurvivors) * e + k)];
+        if (dist < bd) { bd = dist; best = k; }
+    }
+    const size_t slot = size_t(kSurvivors) * e + best;
+    const double *r = d.surv_res + 5 * slot;
+    dm::ClosestPair pair;
+    pair.distance = r[0]; pair.t = r[1]; pair.bary = dm::v(r[2], r[3], r[4]);
+    write_contact(d, e, d.surv_tri[slot], pair);
 }
 
 // ---- contact query without allocation -------------------------------------
@@ -1426,6 +1654,7 @@ __global__ void k_init_scalars(View d)
     d.sc->sweep_fail = kNone;
     d.sc->solve_failed = 0;
     d.sc->pair_count = 0;
+    d.sc->surv_count = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -1585,6 +1814,8 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     const size_t pair_capacity = std::min<size_t>(std::max<size_t>(size_t(1) << 20, 8 * E), size_t(16) << 20);
     bytes += 2 * padded<double>(E) + padded<double>(3 * E) + 2 * padded<uint32_t>(pair_capacity);
     bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E) + padded<double>(6 * E);
+    bytes += padded<float4>(3 * T) + 2 * padded<uint32_t>(size_t(kSurvivors) * E) + padded<uint8_t>(E) +
+             padded<double>(5 * size_t(kSurvivors) * E);
     bytes += 2 * padded<double>(3 * B) + 4 * padded<uint32_t>(B) + padded<int32_t>(B) + 2 * padded<uint32_t>(B) +
              padded<uint32_t>(L) + padded<uint32_t>(T);
     bytes += padded<Partial>(kPartials) + padded<DirPartial>(kPartials) + padded<Scalars>(1);
@@ -1630,6 +1861,9 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.pair_elem = a.take<uint32_t>(pair_capacity); v.pair_tri = a.take<uint32_t>(pair_capacity);
     v.pair_capacity = uint32_t(pair_capacity);
     v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E); v.cache_x = a.take<double>(6 * E);
+    v.tri32 = a.take<float4>(3 * T);
+    v.surv_tri = a.take<uint32_t>(size_t(kSurvivors) * E); v.surv_list = a.take<uint32_t>(size_t(kSurvivors) * E);
+    v.surv_n = a.take<uint8_t>(E); v.surv_res = a.take<double>(5 * size_t(kSurvivors) * E);
     if (E) KHS_CUDA(cudaMemsetAsync(v.cache_n, kCacheInvalid, E, I.stream));
     uint32_t *besc = a.take<uint32_t>(B), *bfirst = a.take<uint32_t>(B), *bcount = a.take<uint32_t>(B);
     v.brefit = a.take<uint32_t>(B);
@@ -1723,6 +1957,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     KHS_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&v.sweep), I.sweep_host, 0));
     v.has_collider = T > 0 ? 1 : 0;
     I.launch("k_init_scalars", k_init_scalars, 1, 1, v);
+    if (T) I.launch("k_tri32", k_tri32, grid_for(T), kBlock, v);
     KHS_CUDA(cudaGetLastError());
     I.original_count = uint32_t(O);
     I.fixed_host = m.fixed;
@@ -1888,8 +2123,12 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
     const bool trial = alpha >= 0.0;
     I.launch(gradient ? "k_node_eval_grad" : "k_node_eval_energy", k_node_eval, grid_for(v.N), kBlock, v, gradient ? 1 : 0,
              trial ? 1 : 0, trial ? alpha : 0.0, dt);
-    if (mode_ && v.has_collider)
-        I.launch("k_contact", k_contact<true>, grid_for(v.E), kBlock, v, static_cast<const double *>(v.q), rebuild_cache_ ? 1 : 0);
+    if (mode_ && v.has_collider) {
+        const double *q = v.q;
+        I.launch("k_contact_filter", k_contact_filter, grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
+        I.launch("k_contact_exact", k_contact_exact, 152 * 4, kBlock, v, q);
+        I.launch("k_contact_select", k_contact_select, grid_for(v.E), kBlock, v);
+    }
     rebuild_cache_ = false;
     I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", mode_ ? k_elem_eval<true> : k_elem_eval<false>, grid_for(v.E),
              kBlock, v, gradient ? 1 : 0);
@@ -2117,6 +2356,7 @@ KhsResult Engine::run_frame(double frame_dt, const double *root_a, const double 
             I.launch("k_begin_substep", k_begin_substep, grid_for(v.N), kBlock, v, root_a, rot_a, root_b, rot_b, f, dt);
             if (v.has_collider) {
                 I.launch("k_collider_interp", k_collider_interp, grid_for(v.V), kBlock, v, I.col_a_copy, col_b, f);
+                I.launch("k_tri32", k_tri32, grid_for(v.T), kBlock, v);
                 I.launch("k_refit", k_refit, grid_for(v.L), kBlock, v, 1);
                 progress_phase_.store(KHS_PHASE_CCD);
                 I.launch("k_sweep", mode_ ? k_sweep<true> : k_sweep<false>, grid_for(v.E), kBlock, v);
