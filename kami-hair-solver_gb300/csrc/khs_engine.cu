@@ -78,6 +78,8 @@ struct Scalars {
     int solve_failed;
     uint32_t pair_count;
     uint32_t surv_count;  // entries of the mixed contact pass's FP64 work list
+    uint32_t solve_next;  // next strand group of the block-solve work queue
+    uint32_t pad;
 };
 
 struct Partial {
@@ -1241,11 +1243,11 @@ __device__ bool inverse6(double a[36], double inv[36])
 // max(1e-12 max|a_ii|, 1e-24) (cuda_backend.cu:855-864).
 constexpr int kSolveGroup = 6, kSolveGroupsPerWarp = 5;
 
-__global__ void __launch_bounds__(128) k_block_solve(View d)
+// One group of kSolveGroupsPerWarp strands (length-sorted order) per warp.
+__device__ __forceinline__ void solve_group(const View &d, uint32_t warp)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int grp = lane / kSolveGroup, r = lane % kSolveGroup, base = grp * kSolveGroup;
     const uint32_t k = warp * kSolveGroupsPerWarp + uint32_t(grp);
     const bool member = grp < kSolveGroupsPerWarp && k < d.S;
@@ -1410,6 +1412,21 @@ __global__ void __launch_bounds__(128) k_block_solve(View d)
     }
 }
 
+// Persistent warps pull strand groups from a queue, longest first, so the
+// long groups that bound the solve do not share a sub-partition's FP64 pipe
+// with a fixed share of the remaining work.
+__global__ void __launch_bounds__(128) k_block_solve(View d)
+{
+    const uint32_t groups = (d.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp;
+    for (;;) {
+        uint32_t g = 0;
+        if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= groups) break;
+        solve_group(d, g);
+    }
+}
+
 
 // Preconditioned steepest descent d = -P g, zero at fixed nodes
 // (cuda_backend.cu:632-638).
@@ -1465,6 +1482,7 @@ __global__ void __launch_bounds__(kBlock) k_final_dir(View d)
         d.sc->ccd_bits = 0x3ff0000000000000ULL;  // 1.0
         d.sc->solve_failed = 0;
         d.sc->pair_count = 0;
+        d.sc->solve_next = 0;
     }
 }
 
@@ -1655,6 +1673,7 @@ __global__ void k_init_scalars(View d)
     d.sc->solve_failed = 0;
     d.sc->pair_count = 0;
     d.sc->surv_count = 0;
+    d.sc->solve_next = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -1710,6 +1729,7 @@ struct Engine::Impl {
     struct KernelStat { const char *name; uint64_t launches; double ms; };
     bool profiling = false;
     uint64_t launches = 0;
+    unsigned solve_blocks = 0;  // launch shape of k_block_solve (0 = not tuned yet)
     std::vector<KernelStat> kstats;
     std::vector<std::pair<size_t, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     std::vector<cudaEvent_t> pool;
@@ -2164,12 +2184,52 @@ void Engine::make_steepest()
     limit_direction(I.mail_host->max_translation);
 }
 
+// Launch shape of the persistent block solve: 1, 2 or 3 blocks of four
+// warps per SM (or fewer when there are fewer strand groups), chosen once
+// by timing each on the first system.  The schedule does not change the
+// result: each strand group is solved by one warp in a fixed order.
+void Engine::tune_block_solve()
+{
+    Impl &I = *d_;
+    const unsigned groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
+    const unsigned most = std::max(1u, (groups + 3) / 4);
+    int sms = 0;
+    KHS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, kDevice));
+    unsigned best = std::min(most, unsigned(sms));
+    float best_ms = 3.0e38f;
+    cudaEvent_t ev[2];
+    KHS_CUDA(cudaEventCreate(&ev[0]));
+    KHS_CUDA(cudaEventCreate(&ev[1]));
+    for (unsigned per_sm = 1; per_sm <= 3; ++per_sm) {
+        const unsigned blocks = std::min(most, per_sm * unsigned(sms));
+        float ms_min = 3.0e38f;
+        for (int rep = 0; rep < 2; ++rep) {
+            KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
+            KHS_CUDA(cudaEventRecord(ev[0], I.stream));
+            k_block_solve<<<blocks, 128, 0, I.stream>>>(I.v);
+            ++I.launches;
+            KHS_CUDA(cudaEventRecord(ev[1], I.stream));
+            KHS_CUDA(cudaEventSynchronize(ev[1]));
+            float ms = 0.0f;
+            KHS_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+            ms_min = std::min(ms_min, ms);
+        }
+        if (ms_min < best_ms) { best_ms = ms_min; best = blocks; }
+        if (blocks == most) break;
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
+    KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_failed, 0, sizeof(int), I.stream));
+    I.solve_blocks = best;
+}
+
 bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
 {
     Impl &I = *d_;
     (void)grad_norm2;
-    const unsigned warps = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
-    I.launch("k_block_solve", k_block_solve, (warps + 3) / 4, 128, I.v);
+    if (!I.solve_blocks) tune_block_solve();
+    I.launch("k_block_solve", k_block_solve, I.solve_blocks, 128, I.v);
     I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
     I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
     I.check();

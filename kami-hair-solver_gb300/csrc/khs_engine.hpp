@@ -100,6 +100,7 @@ private:
     KhsResult optimize_substep(double dt, KhsxSubstepRecord &rec);
     EvalStats evaluate(bool gradient, double dt, double alpha_for_trial);
     bool make_direction(KhsxSubstepRecord &rec, double grad_norm2);
+    void tune_block_solve();
     void make_steepest();
     void limit_direction(double max_translation);
 
