@@ -384,13 +384,22 @@ typedef enum KhsxSolveMode {
        stage a hand-written sm_103a kernel, FP64 throughout. */
     KHSX_MODE_PLAIN_FP64 = 0,
     /* Mixed form: FP32 broadphase (outward-rounded FP32 BVH boxes, exact
-       FP64 re-test at the leaves), FP32-filtered narrow phase and CCD /
-       sweep skip tests with exact FP64 decisions, exact early termination of
-       the CCD advancement.  State, gradient, Gauss-Newton blocks and their
-       factorisation, energies, barrier distances and CCD steps stay FP64:
-       an FP32 block factorisation does not converge under FP64 refinement
-       for these rods (tests/test_fp32_factorization_study.py). */
-    KHSX_MODE_MIXED = 1
+       FP64 re-test at the leaves), FP32-filtered narrow phase with a
+       converged FP64 pass over the survivors, FP32 CCD / sweep skip tests
+       with exact FP64 decisions, exact early termination of the CCD
+       advancement.  State, gradient, Gauss-Newton blocks and their
+       factorisation, energies, barrier distances and CCD steps stay FP64,
+       so its results equal the plain form's bit for bit.  (A plain FP32
+       block factorisation does not converge under FP64 refinement for these
+       rods: tests/test_fp32_factorization_study.py.) */
+    KHSX_MODE_MIXED = 1,
+    /* Mixed form with a float-float (two FP32 words, about 48 bits)
+       block-tridiagonal factorisation and FP64 iterative refinement on the
+       Gauss-Newton residual: sweeps repeat (at most 3) while a strand's
+       relative correction exceeds 1e-4; a float-float pivot failure falls
+       back to the FP64 factorisation (KhsxSubstepRecord.fp64_fallbacks).
+       Directions differ from the plain form's by rounding only. */
+    KHSX_MODE_MIXED_FF = 2
 } KhsxSolveMode;
 
 /* Selects the solve form.  May be called before or after khsBuild. */
@@ -411,8 +420,8 @@ typedef struct KhsxSubstepRecord {
     uint32_t newton_iterations;
     uint32_t line_search_evaluations;
     uint32_t steepest_fallbacks;
-    uint32_t refinement_sweeps;    /* reserved (always 0, see KHSX_MODE_MIXED) */
-    uint32_t fp64_fallbacks;       /* reserved (always 0) */
+    uint32_t refinement_sweeps;    /* KHSX_MODE_MIXED_FF: FP64 refinement sweeps */
+    uint32_t fp64_fallbacks;       /* KHSX_MODE_MIXED_FF: directions re-solved in FP64 */
     uint32_t reserved;
     uint64_t contact_candidates;
     uint64_t active_contacts;

@@ -606,7 +606,7 @@ KHS_API const char *khsGetLastError(const KhsSolver *s)
 
 KHS_API KhsResult khsxSetSolveMode(KhsSolver *s, uint32_t mode)
 {
-    if (!s || mode > KHSX_MODE_MIXED) return KHS_ERROR_INVALID_ARGUMENT;
+    if (!s || mode > KHSX_MODE_MIXED_FF) return KHS_ERROR_INVALID_ARGUMENT;
     s->mode = mode;
     if (s->engine) s->engine->set_mode(mode);
     return KHS_OK;

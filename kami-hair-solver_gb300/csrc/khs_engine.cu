@@ -26,6 +26,7 @@
 //   block over the partials) and therefore deterministic.
 #include "khs_engine.hpp"
 #include "khs_device_math.cuh"
+#include "khs_ff.cuh"
 
 #include <cuda_runtime.h>
 
@@ -68,6 +69,8 @@ struct Mailbox {
     unsigned long long ccd_bits;
     uint32_t sweep_fail;
     uint32_t pair_count;
+    uint32_t refine_bits;
+    uint32_t pad;
 };
 
 // Atomic targets live in device memory; the publishing kernels copy them to
@@ -79,7 +82,7 @@ struct Scalars {
     uint32_t pair_count;
     uint32_t surv_count;  // entries of the mixed contact pass's FP64 work list
     uint32_t solve_next;  // next strand group of the block-solve work queue
-    uint32_t pad;
+    uint32_t refine_bits; // largest relative refinement correction (FP32 bits)
 };
 
 struct Partial {
@@ -140,6 +143,10 @@ struct View {
     // kSurvivors, in traversal order), their FP64 closest pairs (distance,
     // t, barycentrics) and the (element, slot) work list of the FP64 pass.
     float4 *tri32;
+    // Mixed-form factors in float-float (hi, lo): B_n^-1 and C_n rows [N][36],
+    // d'_n [N][6], and the diagonal shift used at each node.
+    float2 *ff_inv, *ff_c, *ff_d;
+    float *ff_shift;
     uint32_t *surv_tri, *surv_list;
     uint8_t *surv_n;
     double *surv_res;
@@ -1428,6 +1435,326 @@ __global__ void __launch_bounds__(128) k_block_solve(View d)
 }
 
 
+// ---- mixed form: float-float block solve with FP64 refinement -------------
+//
+// The same block Thomas recurrence as k_block_solve (per strand, one lane
+// per block row, Gauss-Jordan with partial pivoting on the first largest
+// |pivot|, relative diagonal shift) evaluated in float-float arithmetic:
+// k_ff_factor stores B_n^-1, C_n = B_n^-1 U_n and d'_n and writes the first
+// direction; k_ff_residual forms r = -g - A x in FP64 (one thread per row,
+// no sequential chain), with the shifts the factorisation used; k_ff_correct
+// solves A delta = r with the stored factors and adds delta to the direction
+// in FP64.  The float-float factor has about 48 significant bits, so a sweep
+// contracts the error by about cond(B) * 2^-48 and one sweep recovers the
+// accuracy of the FP64 solve for the condition numbers of these systems
+// (block condition numbers up to about 1e10); further sweeps run while the
+// largest relative correction of any strand exceeds kRefineRatio.  A pivot
+// below 1e-30 or a value outside the FP32 exponent range sets the solve
+// failure flag and the host falls back to k_block_solve.
+
+constexpr float kRefineRatio = 1.0e-4f;
+constexpr int kRefineSweepsMax = 3;
+
+__device__ __forceinline__ void group_range(const View &d, uint32_t warp, int lane, int &r, int &base, uint32_t &begin,
+                                            uint32_t &len, uint32_t &maxlen)
+{
+    const int grp = lane / kSolveGroup;
+    r = lane % kSolveGroup;
+    base = grp * kSolveGroup;
+    const uint32_t k = warp * kSolveGroupsPerWarp + uint32_t(grp);
+    const bool member = grp < kSolveGroupsPerWarp && k < d.S;
+    begin = 0; len = 0;
+    if (member) {
+        const uint32_t s = d.sorder[k];
+        begin = d.sfirst[s] + d.sfixed[s];
+        const uint32_t end = d.sfirst[s] + d.scount[s];
+        len = end > begin ? end - begin : 0;
+    }
+    maxlen = len;
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+}
+
+__device__ __forceinline__ float2 f2(ff::FF a) { return make_float2(a.hi, a.lo); }
+__device__ __forceinline__ ff::FF fromf2(float2 a) { return ff::make(a.x, a.y); }
+
+__device__ __forceinline__ void ff_factor_group(const View &d, uint32_t warp)
+{
+    const int lane = threadIdx.x & 31;
+    int r, base;
+    uint32_t begin, len, maxlen;
+    group_range(d, warp, lane, r, base, begin, len, maxlen);
+    double nd[6], nu[6], nuc[6], ng = 0.0;
+    auto fetch = [&](uint32_t t) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) nd[c] = on ? d.diag[36 * n + 6 * r + c] : 0.0;
+        ng = on ? d.grad[6 * n + r] : 0.0;
+        const bool up = on && t + 1 < len;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) nu[c] = up ? d.upper[36 * n + 6 * r + c] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) nuc[q] = (on && t > 0) ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
+    };
+    fetch(0);
+    ff::FF Crow[6], dprev = ff::make(0.0f);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) Crow[c] = ff::make(0.0f);
+    bool failed = false;
+    for (uint32_t t = 0; t < maxlen; ++t) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        bool bad = false;
+        ff::FF a[6], inv[6], urow[6], ucol[6];
+        ff::FF rhs = ff::neg(ff::split(ng, bad));
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            a[c] = ff::split(nd[c], bad);
+            inv[c] = ff::make(c == r ? 1.0f : 0.0f);
+            ucol[c] = ff::split(nuc[c], bad);
+            urow[c] = ff::split(nu[c], bad);
+        }
+        if (t + 1 < maxlen) fetch(t + 1);
+        if (t > 0) {
+            // B = D - U_{n-1}^T C_{n-1}, rhs = -g - U_{n-1}^T d'_{n-1}
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) a[c] = ff::fms(a[c], ucol[q], ff::shfl(Crow[c], base + q));
+                rhs = ff::fms(rhs, ucol[q], ff::shfl(dprev, base + q));
+            }
+        }
+        // Relative diagonal shift max(1e-12 max|b_ii|, 1e-24); the value used
+        // is stored for the FP64 residual.
+        ff::FF diag_r = ff::make(0.0f);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) if (c == r) diag_r = a[c];
+        unsigned smax = 0u;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) smax = max(smax, __shfl_sync(0xffffffffu, ff::abs_bits(diag_r), base + q));
+        const float shift = fmaxf(__fmul_rn(1.0e-12f, __uint_as_float(smax)), 1.0e-24f);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) if (c == r) a[c] = ff::add(a[c], ff::make(shift));
+        if (on && r == 0) d.ff_shift[n] = shift;
+        bool ok = !bad;
+#pragma unroll
+        for (int col = 0; col < 6; ++col) {
+            ff::FF mine = ff::make(0.0f);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) if (c == col) mine = a[c];
+            const unsigned mb = ff::abs_bits(mine);
+            int pivot = col;
+            unsigned best = __shfl_sync(0xffffffffu, mb, base + col);
+#pragma unroll
+            for (int row = col + 1; row < 6; ++row) {
+                const unsigned vrow = __shfl_sync(0xffffffffu, mb, base + row);
+                if (vrow > best) { best = vrow; pivot = row; }
+            }
+            // best < 1e-30 or not finite => failure.
+            if (best < 0x0da24260u || best >= 0x7f800000u) ok = false;
+            const int partner = r == col ? pivot : (r == pivot ? col : r);
+#pragma unroll
+            for (int c = col; c < 6; ++c) a[c] = ff::shfl(a[c], base + partner);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) inv[c] = ff::shfl(inv[c], base + partner);
+            ff::FF pv = ff::make(1.0f);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) if (c == col) pv = a[c];
+            const ff::FF ip = ff::rcp(ff::shfl(pv, base + col));
+            ff::FF f = ff::make(0.0f);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) if (c == col) f = a[c];
+#pragma unroll
+            for (int c = col + 1; c < 6; ++c) {
+                const ff::FF p = ff::mul(ff::shfl(a[c], base + col), ip);
+                a[c] = (r == col) ? p : ff::fms(a[c], f, p);
+            }
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const ff::FF p = ff::mul(ff::shfl(inv[c], base + col), ip);
+                inv[c] = (r == col) ? p : ff::fms(inv[c], f, p);
+            }
+        }
+        if (on && !ok) {
+            failed = true;
+            if (r == 0) atomicExch(&d.sc->solve_failed, 1);
+        }
+        // C_n = B^-1 U_n, d'_n = B^-1 rhs (row q of U_n in lane q).
+        ff::FF dn = ff::make(0.0f);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) Crow[c] = ff::make(0.0f);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) Crow[c] = ff::fma(Crow[c], inv[q], ff::shfl(urow[c], base + q));
+            dn = ff::fma(dn, inv[q], ff::shfl(rhs, base + q));
+        }
+        dprev = dn;
+        if (on && !failed) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                d.ff_inv[36 * n + 6 * r + c] = f2(inv[c]);
+                d.ff_c[36 * n + 6 * r + c] = f2(Crow[c]);
+            }
+            d.ff_d[6 * n + r] = f2(dn);
+        }
+    }
+    // Back substitution x_n = d'_n - C_n x_{n+1}.
+    ff::FF next = ff::make(0.0f), pc[6], pd = ff::make(0.0f);
+    auto fetch_back = [&](uint32_t t) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        pd = on ? fromf2(d.ff_d[6 * n + r]) : ff::make(0.0f);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) pc[q] = on ? fromf2(d.ff_c[36 * n + 6 * r + q]) : ff::make(0.0f);
+    };
+    if (maxlen) fetch_back(maxlen - 1);
+    for (uint32_t t = maxlen; t-- > 0;) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        ff::FF value = pd, crow[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) crow[q] = pc[q];
+        if (t > 0) fetch_back(t - 1);
+        const bool coupled = on && t + 1 < len;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const ff::FF xq = ff::shfl(next, base + q);
+            if (coupled) value = ff::fms(value, crow[q], xq);
+        }
+        if (on) d.dir[6 * n + r] = ff::to_double(value);
+        next = on ? value : ff::make(0.0f);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_ff_factor(View d)
+{
+    const uint32_t groups = (d.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp;
+    for (;;) {
+        uint32_t g = 0;
+        if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= groups) break;
+        ff_factor_group(d, g);
+    }
+}
+
+// r = -g - (A + shifts) x in FP64, one thread per row of a free node.
+__global__ void __launch_bounds__(kBlock) k_ff_residual(View d)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.sc->solve_next = 0;  // k_ff_factor has completed
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 6 * d.N) return;
+    const uint32_t n = idx / 6, r = idx % 6;
+    if (d.fixed[n]) { d.dprime[idx] = 0.0; return; }
+    const double *x = d.dir + 6 * size_t(n);
+    const double *D = d.diag + 36 * size_t(n) + 6 * r;
+    double res = -d.grad[idx] - double(d.ff_shift[n]) * x[r];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) res -= D[c] * x[c];
+    if (d.elem_right[n] >= 0) {
+        const double *U = d.upper + 36 * size_t(n) + 6 * r, *xn = x + 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) res -= U[c] * xn[c];
+    }
+    if (d.elem_left[n] >= 0 && !d.fixed[n - 1]) {
+        const double *U = d.upper + 36 * size_t(n - 1) + r, *xp = x - 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) res -= U[6 * c] * xp[c];
+    }
+    d.dprime[idx] = res;
+}
+
+__device__ __forceinline__ void ff_correct_group(const View &d, uint32_t warp)
+{
+    const int lane = threadIdx.x & 31;
+    int r, base;
+    uint32_t begin, len, maxlen;
+    group_range(d, warp, lane, r, base, begin, len, maxlen);
+    double nres = 0.0, nuc[6];
+    float2 ninv[6];
+    auto fetch = [&](uint32_t t) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+        nres = on ? d.dprime[6 * n + r] : 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) ninv[c] = on ? d.ff_inv[36 * n + 6 * r + c] : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) nuc[q] = (on && t > 0) ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
+    };
+    fetch(0);
+    ff::FF dprev = ff::make(0.0f);
+    for (uint32_t t = 0; t < maxlen; ++t) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+        bool bad = false;
+        ff::FF rhs = ff::split(nres, bad), inv[6], ucol[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { inv[c] = fromf2(ninv[c]); ucol[c] = ff::split(nuc[c], bad); }
+        if (t + 1 < maxlen) fetch(t + 1);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) rhs = ff::fms(rhs, ucol[q], ff::shfl(dprev, base + q));
+        ff::FF dn = ff::make(0.0f);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) dn = ff::fma(dn, inv[q], ff::shfl(rhs, base + q));
+        dprev = dn;
+        if (on) d.ff_d[6 * n + r] = f2(dn);
+    }
+    ff::FF next = ff::make(0.0f), pc[6], pd = ff::make(0.0f);
+    auto fetch_back = [&](uint32_t t) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+        pd = on ? fromf2(d.ff_d[6 * n + r]) : ff::make(0.0f);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) pc[q] = on ? fromf2(d.ff_c[36 * n + 6 * r + q]) : ff::make(0.0f);
+    };
+    if (maxlen) fetch_back(maxlen - 1);
+    float dmax = 0.0f, xmax = 0.0f;
+    for (uint32_t t = maxlen; t-- > 0;) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+        ff::FF value = pd, crow[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) crow[q] = pc[q];
+        if (t > 0) fetch_back(t - 1);
+        const bool coupled = on && t + 1 < len;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const ff::FF xq = ff::shfl(next, base + q);
+            if (coupled) value = ff::fms(value, crow[q], xq);
+        }
+        if (on) {
+            const double x = d.dir[6 * n + r] + ff::to_double(value);
+            d.dir[6 * n + r] = x;
+            dmax = fmaxf(dmax, fabsf(value.hi));
+            xmax = fmaxf(xmax, fabsf(float(x)));
+        }
+        next = on ? value : ff::make(0.0f);
+    }
+    // Largest relative correction of the strand (over its rows) for the
+    // host's sweep decision.
+    for (int o = 16; o > 0; o >>= 1) {
+        dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        xmax = fmaxf(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+    }
+    if (lane == 0 && dmax > 0.0f) {
+        const float ratio = xmax > 0.0f ? dmax / xmax : 3.0e38f;
+        atomicMax(&d.sc->refine_bits, __float_as_uint(ratio));
+    }
+}
+
+__global__ void __launch_bounds__(128) k_ff_correct(View d)
+{
+    const uint32_t groups = (d.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp;
+    for (;;) {
+        uint32_t g = 0;
+        if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= groups) break;
+        ff_correct_group(d, g);
+    }
+}
+
 // Preconditioned steepest descent d = -P g, zero at fixed nodes
 // (cuda_backend.cu:632-638).
 __global__ void __launch_bounds__(kBlock) k_steepest(View d)
@@ -1479,10 +1806,12 @@ __global__ void __launch_bounds__(kBlock) k_final_dir(View d)
         d.mail->ccd_bits = d.sc->ccd_bits;
         d.mail->solve_failed = d.sc->solve_failed;
         d.mail->pair_count = d.sc->pair_count;
+        d.mail->refine_bits = d.sc->refine_bits;
         d.sc->ccd_bits = 0x3ff0000000000000ULL;  // 1.0
         d.sc->solve_failed = 0;
         d.sc->pair_count = 0;
         d.sc->solve_next = 0;
+        d.sc->refine_bits = 0;
     }
 }
 
@@ -1674,6 +2003,7 @@ __global__ void k_init_scalars(View d)
     d.sc->pair_count = 0;
     d.sc->surv_count = 0;
     d.sc->solve_next = 0;
+    d.sc->refine_bits = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -1834,6 +2164,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     const size_t pair_capacity = std::min<size_t>(std::max<size_t>(size_t(1) << 20, 8 * E), size_t(16) << 20);
     bytes += 2 * padded<double>(E) + padded<double>(3 * E) + 2 * padded<uint32_t>(pair_capacity);
     bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E) + padded<double>(6 * E);
+    bytes += 2 * padded<float2>(36 * N) + padded<float2>(6 * N) + padded<float>(N);
     bytes += padded<float4>(3 * T) + 2 * padded<uint32_t>(size_t(kSurvivors) * E) + padded<uint8_t>(E) +
              padded<double>(5 * size_t(kSurvivors) * E);
     bytes += 2 * padded<double>(3 * B) + 4 * padded<uint32_t>(B) + padded<int32_t>(B) + 2 * padded<uint32_t>(B) +
@@ -1882,6 +2213,8 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.pair_capacity = uint32_t(pair_capacity);
     v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E); v.cache_x = a.take<double>(6 * E);
     v.tri32 = a.take<float4>(3 * T);
+    v.ff_inv = a.take<float2>(36 * N); v.ff_c = a.take<float2>(36 * N); v.ff_d = a.take<float2>(6 * N);
+    v.ff_shift = a.take<float>(N);
     v.surv_tri = a.take<uint32_t>(size_t(kSurvivors) * E); v.surv_list = a.take<uint32_t>(size_t(kSurvivors) * E);
     v.surv_n = a.take<uint8_t>(E); v.surv_res = a.take<double>(5 * size_t(kSurvivors) * E);
     if (E) KHS_CUDA(cudaMemsetAsync(v.cache_n, kCacheInvalid, E, I.stream));
@@ -2229,12 +2562,37 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
     Impl &I = *d_;
     (void)grad_norm2;
     if (!I.solve_blocks) tune_block_solve();
-    I.launch("k_block_solve", k_block_solve, I.solve_blocks, 128, I.v);
-    I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
-    I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
-    I.check();
-    I.sync();
     const Mailbox &mb = *I.mail_host;
+    bool fp64 = mode_ != KHSX_MODE_MIXED_FF;
+    if (!fp64) {
+        I.launch("k_ff_factor", k_ff_factor, I.solve_blocks, 128, I.v);
+        uint32_t sweeps = 0;
+        for (;;) {
+            I.launch("k_ff_residual", k_ff_residual, grid_for(6 * size_t(I.v.N)), kBlock, I.v);
+            I.launch("k_ff_correct", k_ff_correct, I.solve_blocks, 128, I.v);
+            ++sweeps;
+            I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
+            I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
+            I.check();
+            I.sync();
+            if (mb.solve_failed) break;
+            float ratio;
+            std::memcpy(&ratio, &mb.refine_bits, sizeof(ratio));
+            if (!(ratio > kRefineRatio) || sweeps >= uint32_t(kRefineSweepsMax)) break;
+        }
+        rec.refinement_sweeps += sweeps;
+        if (mb.solve_failed) {
+            ++rec.fp64_fallbacks;
+            fp64 = true;
+        }
+    }
+    if (fp64) {
+        I.launch("k_block_solve", k_block_solve, I.solve_blocks, 128, I.v);
+        I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
+        I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
+        I.check();
+        I.sync();
+    }
     const bool used = !mb.solve_failed && mb.slope < 0 && std::isfinite(mb.slope);
     if (!used) {
         ++rec.steepest_fallbacks;

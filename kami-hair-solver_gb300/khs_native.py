@@ -37,6 +37,7 @@ FAILURE_NONE, FAILURE_SWEEP, FAILURE_BARRIER_INFEASIBLE, FAILURE_NONLINEAR_SOLVE
 
 MODE_PLAIN_FP64 = 0
 MODE_MIXED = 1
+MODE_MIXED_FF = 2
 
 PACKAGE_DIR = Path(__file__).resolve().parent
 DEFAULT_LIBRARY = PACKAGE_DIR / "_build" / "libkami_hair_solver.so"

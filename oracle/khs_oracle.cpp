@@ -2044,7 +2044,7 @@ KHS_API const char *khsGetLastError(const KhsSolver *s)
     return s ? s->impl.error_.c_str() : invalid;
 }
 
-KHS_API KhsResult khsxSetSolveMode(KhsSolver *s, uint32_t mode) { return s && mode <= 1 ? KHS_OK : KHS_ERROR_INVALID_ARGUMENT; }
+KHS_API KhsResult khsxSetSolveMode(KhsSolver *s, uint32_t mode) { return s && mode <= 2 ? KHS_OK : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API uint32_t khsxGetSolveMode(const KhsSolver *) { return 0; }
 KHS_API KhsResult khsxCopyState(const KhsSolver *s, double *q, double *v, uint64_t cap) { return s ? s->impl.copy_state(q, v, cap) : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API uint32_t khsxGetSubstepRecordCount(const KhsSolver *s) { return s ? s->impl.record_count() : 0; }
