@@ -406,6 +406,14 @@ typedef enum KhsxSolveMode {
 KHS_API KhsResult khsxSetSolveMode(KhsSolver *solver, uint32_t mode);
 KHS_API uint32_t khsxGetSolveMode(const KhsSolver *solver);
 
+/* Launch shape of the FP64 block-tridiagonal solve.  By default it is tuned
+   once per solver by timing each shape on the first system; this pins it:
+   strands_per_warp 5 (6 lanes per strand) or 2 (12 lanes per strand, half
+   the instructions on each strand's sequential chain), blocks_per_sm 1-8.
+   strands_per_warp 0 restores the tuning.  Every shape gives bit-identical
+   directions.  Requires a built solver. */
+KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *solver, uint32_t strands_per_warp, uint32_t blocks_per_sm);
+
 /* Copies the full generalised state: q and v are 6 * internal_node_count
    FP64 values each, per-node interleaved (x, y, z, rx, ry, rz).  Either
    pointer may be NULL. */

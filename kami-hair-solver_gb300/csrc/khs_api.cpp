@@ -614,6 +614,14 @@ KHS_API KhsResult khsxSetSolveMode(KhsSolver *s, uint32_t mode)
 
 KHS_API uint32_t khsxGetSolveMode(const KhsSolver *s) { return s ? s->mode : 0; }
 
+KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *s, uint32_t strands_per_warp, uint32_t blocks_per_sm)
+{
+    return guarded(s, [&] {
+        if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+        return s->engine->set_block_solve_schedule(strands_per_warp, blocks_per_sm);
+    });
+}
+
 KHS_API KhsResult khsxCopyState(const KhsSolver *s, double *q, double *v, uint64_t dof_capacity)
 {
     if (!s || !s->built || !s->engine) return KHS_ERROR_INVALID_ARGUMENT;

@@ -20,7 +20,7 @@
 // Kernels (one thread per node / element / strand / BVH leaf):
 //   k_begin_substep, k_collider_interp, k_refit, k_sweep(+record),
 //   k_precond, k_node_eval, k_elem_eval, k_node_sum, k_reduce_eval,
-//   k_final_eval, k_block_solve, k_steepest, k_scale, k_reduce_dir,
+//   k_final_eval, k_block_solve_aug, k_steepest, k_scale, k_reduce_dir,
 //   k_final_dir, k_ccd, k_update_velocity, k_friction, k_friction_apply,
 //   k_gather.  Reductions are two-level (fixed per-block trees, then one
 //   block over the partials) and therefore deterministic.
@@ -1239,25 +1239,42 @@ __device__ bool inverse6(double a[36], double inv[36])
     return true;
 }
 
-// Block-tridiagonal Thomas solve per strand (cuda_backend.cu:866-881),
-// row-parallel: a group of 6 lanes owns one strand and lane r holds row r of
-// every 6x6 block (B, its Gauss-Jordan inverse, C = B^-1 U), so a warp
-// solves 5 strands at once and the 6x6 algebra runs on 30 lanes with
-// shuffles for the pivot search, row swaps and row broadcasts.  Strands are
-// taken in length-sorted order so the 5 strands of a warp have similar
-// lengths.  The inverse is the reference's Gauss-Jordan elimination with
-// partial pivoting (first largest pivot) after the relative diagonal shift
-// max(1e-12 max|a_ii|, 1e-24) (cuda_backend.cu:855-864).
-constexpr int kSolveGroup = 6, kSolveGroupsPerWarp = 5;
+// Block-tridiagonal Thomas solve per strand (cuda_backend.cu:866-881) with
+// the reference's Gauss-Jordan elimination, partial pivoting on the first
+// largest |pivot|, after the relative diagonal shift max(1e-12 max|a_ii|,
+// 1e-24) (cuda_backend.cu:855-864).  Strands are taken in length-sorted
+// order, longest first, by persistent warps from a work queue, so the
+// strands of a warp have similar lengths and the long strands that bound
+// the solve start first.
+constexpr int kSolveGroup = 6, kSolveGroupsPerWarp = 5;  // float-float kernels: 6 lanes per strand, 5 per warp
 
-// One group of kSolveGroupsPerWarp strands (length-sorted order) per warp.
-__device__ __forceinline__ void solve_group(const View &d, uint32_t warp)
+// Block Thomas solve with Gauss-Jordan elimination on the augmented block
+// [B_n | U_n | rhs_n]: the elimination leaves C_n = B_n^-1 U_n and
+// d'_n = B_n^-1 rhs_n in place of U_n and rhs_n (the reference forms
+// B_n^-1 first and multiplies; the operations per result entry differ in
+// order only).  Finished pivot columns are not updated.  A group of 6 H lanes
+// owns one strand: lane (r, h) holds row r, columns [6h/H, 6(h+1)/H) of B_n
+// and U_n; every lane of row r holds rhs_n[r].  H = 1 puts 5 strands in a
+// warp, H = 2 puts 2 strands in a warp and halves the instructions on each
+// strand's sequential chain.  Every entry is computed by the same sequence
+// of operations in both layouts, so the results are identical bit for bit
+// and the launch tuner may pick either.
+template<int H> struct AugLayout {
+    static constexpr int kCols = 6 / H;              // columns per lane
+    static constexpr int kLanes = 6 * H;             // lanes per strand
+    static constexpr int kStrands = 32 / kLanes;     // strands per warp
+};
+
+template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, uint32_t g)
 {
+    using L = AugLayout<H>;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int grp = lane / kSolveGroup, r = lane % kSolveGroup, base = grp * kSolveGroup;
-    const uint32_t k = warp * kSolveGroupsPerWarp + uint32_t(grp);
-    const bool member = grp < kSolveGroupsPerWarp && k < d.S;
+    const int grp = lane / L::kLanes, gl = lane % L::kLanes, r = gl % 6, h = gl / 6;
+    const int base = grp * L::kLanes;
+    const int c0 = h * L::kCols;  // first column of this lane
+    const uint32_t k = g * L::kStrands + uint32_t(grp);
+    const bool member = grp < L::kStrands && k < d.S;
     uint32_t begin = 0, len = 0;
     if (member) {
         const uint32_t s = d.sorder[k];
@@ -1267,130 +1284,123 @@ __device__ __forceinline__ void solve_group(const View &d, uint32_t warp)
     }
     uint32_t maxlen = len;
     for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(FULL, maxlen, o));
-    // The inputs of node t + 1 (its diagonal block row, gradient entry, the
-    // coupling block to t + 2 and the column of U_t) are loaded while node t
-    // is being eliminated, so the memory latency stays off the sequential
-    // chain along the strand.
-    double nd[6], nu[6], nuc[6], ng = 0.0;
+    double nd[L::kCols], nu[L::kCols], nuc[6], ng = 0.0;
     auto fetch = [&](uint32_t t) {
         const bool on = t < len;
         const size_t n = begin + t;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) nd[c] = on ? d.diag[36 * n + 6 * r + c] : 0.0;
+        for (int j = 0; j < L::kCols; ++j) nd[j] = on ? d.diag[36 * n + 6 * r + c0 + j] : 0.0;
         ng = on ? d.grad[6 * n + r] : 0.0;
         const bool up = on && t + 1 < len;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) nu[c] = up ? d.upper[36 * n + 6 * r + c] : 0.0;
+        for (int j = 0; j < L::kCols; ++j) nu[j] = up ? d.upper[36 * n + 6 * r + c0 + j] : 0.0;
 #pragma unroll
         for (int q = 0; q < 6; ++q) nuc[q] = (on && t > 0) ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
     };
     fetch(0);
-    double Crow[6] = {0, 0, 0, 0, 0, 0}, dprev = 0.0;
+    double Cprev[L::kCols], dprev = 0.0;
+#pragma unroll
+    for (int j = 0; j < L::kCols; ++j) Cprev[j] = 0.0;
     bool failed = false;
     for (uint32_t t = 0; t < maxlen; ++t) {
         const bool on = t < len && !failed;
         const size_t n = begin + t;
-        double a[6], inv[6], urow[6], ucol[6], rhs = -ng;
+        double a[L::kCols], u[L::kCols], ucol[6], rhs = -ng;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) { a[c] = nd[c]; inv[c] = (c == r) ? 1.0 : 0.0; ucol[c] = nuc[c]; urow[c] = nu[c]; }
+        for (int j = 0; j < L::kCols; ++j) { a[j] = nd[j]; u[j] = nu[j]; }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) ucol[q] = nuc[q];
         if (t + 1 < maxlen) fetch(t + 1);
         if (t > 0) {
             // B -= U_{n-1}^T C_{n-1}, rhs -= U_{n-1}^T d'_{n-1}
-            double sum[6] = {0, 0, 0, 0, 0, 0}, sr = 0.0;
+            double sum[L::kCols], sr = 0.0;
+#pragma unroll
+            for (int j = 0; j < L::kCols; ++j) sum[j] = 0.0;
 #pragma unroll
             for (int q = 0; q < 6; ++q) {
 #pragma unroll
-                for (int c = 0; c < 6; ++c) sum[c] += ucol[q] * __shfl_sync(FULL, Crow[c], base + q);
-                sr += ucol[q] * __shfl_sync(FULL, dprev, base + q);
+                for (int j = 0; j < L::kCols; ++j) sum[j] = __fma_rn(ucol[q], __shfl_sync(FULL, Cprev[j], base + 6 * h + q), sum[j]);
+                sr = __fma_rn(ucol[q], __shfl_sync(FULL, dprev, base + q), sr);
             }
 #pragma unroll
-            for (int c = 0; c < 6; ++c) a[c] -= sum[c];
-            rhs -= sr;
+            for (int j = 0; j < L::kCols; ++j) a[j] = __dsub_rn(a[j], sum[j]);
+            rhs = __dsub_rn(rhs, sr);
         }
-        // Relative diagonal shift max(1e-12 max|a_ii|, 1e-24).
+        // Relative diagonal shift max(1e-12 max|b_ii|, 1e-24).
         double diag_r = 0.0;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) if (c == r) diag_r = a[c];
-        // |x| of a double compares like its sign-cleared bit pattern, so the
-        // maxima below are integer operations.
+        for (int j = 0; j < L::kCols; ++j) if (c0 + j == r) diag_r = a[j];
         unsigned long long smax = 0ull;
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
-            const unsigned long long b = (unsigned long long)__double_as_longlong(__shfl_sync(FULL, diag_r, base + q)) & 0x7fffffffffffffffull;
+            const int owner = base + 6 * (q / L::kCols) + q;
+            const unsigned long long b = (unsigned long long)__double_as_longlong(__shfl_sync(FULL, diag_r, owner)) & 0x7fffffffffffffffull;
             smax = b > smax ? b : smax;
         }
-        const double shift = fmax(1.0e-12 * __longlong_as_double((long long)smax), 1.0e-24);
+        const double shift = fmax(__dmul_rn(1.0e-12, __longlong_as_double((long long)smax)), 1.0e-24);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) if (c == r) a[c] += shift;
-        // Gauss-Jordan with partial pivoting (first largest |pivot|).
+        for (int j = 0; j < L::kCols; ++j) if (c0 + j == r) a[j] = __dadd_rn(a[j], shift);
         bool ok = true;
 #pragma unroll
         for (int col = 0; col < 6; ++col) {
-            double mine = 0.0;
+            const int hc = col / L::kCols, jc = col % L::kCols;
+            const int owner_half = base + 6 * hc;
+            double acol = 0.0;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) if (c == col) mine = a[c];
-            const unsigned long long mb = (unsigned long long)__double_as_longlong(mine) & 0x7fffffffffffffffull;
+            for (int j = 0; j < L::kCols; ++j) if (j == jc && h == hc) acol = a[j];
+            const unsigned long long mb = (unsigned long long)__double_as_longlong(acol) & 0x7fffffffffffffffull;
             int pivot = col;
-            unsigned long long best = __shfl_sync(FULL, mb, base + col);
+            unsigned long long best = __shfl_sync(FULL, mb, owner_half + col);
 #pragma unroll
             for (int row = col + 1; row < 6; ++row) {
-                const unsigned long long vrow = __shfl_sync(FULL, mb, base + row);
+                const unsigned long long vrow = __shfl_sync(FULL, mb, owner_half + row);
                 if (vrow > best) { best = vrow; pivot = row; }
             }
             // best < 1e-30 or not finite (exponent all ones) => failure.
             if (best < 0x39b4484bfeebc2a0ull || best >= 0x7ff0000000000000ull) ok = false;
             const int partner = r == col ? pivot : (r == pivot ? col : r);
+            const int src = base + 6 * h + partner;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                a[c] = __shfl_sync(FULL, a[c], base + partner);
-                inv[c] = __shfl_sync(FULL, inv[c], base + partner);
+            for (int j = 0; j < L::kCols; ++j) {
+                a[j] = __shfl_sync(FULL, a[j], src);
+                u[j] = __shfl_sync(FULL, u[j], src);
             }
-            double pv = 0.0;
+            rhs = __shfl_sync(FULL, rhs, src);
+            acol = 0.0;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) if (c == col) pv = a[c];
-            const double ip = 1.0 / __shfl_sync(FULL, pv, base + col);
-            double prow[6], pinv[6];
+            for (int j = 0; j < L::kCols; ++j) if (j == jc && h == hc) acol = a[j];
+            const double ip = __drcp_rn(__shfl_sync(FULL, acol, owner_half + col));
+            const double f = __shfl_sync(FULL, acol, owner_half + r);
+            const int prow = base + 6 * h + col;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                prow[c] = __shfl_sync(FULL, a[c], base + col) * ip;
-                pinv[c] = __shfl_sync(FULL, inv[c], base + col) * ip;
+            for (int j = 0; j < L::kCols; ++j) {
+                if (H == 1 && j <= col) continue;  // finished columns (H = 1: known at compile time)
+                const double p = __dmul_rn(__shfl_sync(FULL, a[j], prow), ip);
+                a[j] = (r == col) ? p : __fma_rn(-f, p, a[j]);
             }
-            if (r == col) {
 #pragma unroll
-                for (int c = 0; c < 6; ++c) { a[c] = prow[c]; inv[c] = pinv[c]; }
-            } else {
-                double f = 0.0;
-#pragma unroll
-                for (int c = 0; c < 6; ++c) if (c == col) f = a[c];
-#pragma unroll
-                for (int c = 0; c < 6; ++c) { a[c] -= f * prow[c]; inv[c] -= f * pinv[c]; }
+            for (int j = 0; j < L::kCols; ++j) {
+                const double p = __dmul_rn(__shfl_sync(FULL, u[j], prow), ip);
+                u[j] = (r == col) ? p : __fma_rn(-f, p, u[j]);
             }
+            const double pr = __dmul_rn(__shfl_sync(FULL, rhs, prow), ip);
+            rhs = (r == col) ? pr : __fma_rn(-f, pr, rhs);
         }
         if (on && !ok) {
             failed = true;
-            if (r == 0) atomicExch(&d.sc->solve_failed, 1);
+            if (gl == 0) atomicExch(&d.sc->solve_failed, 1);
         }
-        // C_n = B^-1 U_n (zero at the strand tip), d'_n = B^-1 rhs.
-        // (row q of U_n lives in lane q of the group)
-        double csum[6] = {0, 0, 0, 0, 0, 0};
+        // u now holds row r of C_n (zero at the strand tip), rhs = d'_n[r].
 #pragma unroll
-        for (int q = 0; q < 6; ++q)
-#pragma unroll
-            for (int c = 0; c < 6; ++c) csum[c] += inv[q] * __shfl_sync(FULL, urow[c], base + q);
-#pragma unroll
-        for (int c = 0; c < 6; ++c) Crow[c] = csum[c];
-        double dn = 0.0;
-#pragma unroll
-        for (int q = 0; q < 6; ++q) dn += inv[q] * __shfl_sync(FULL, rhs, base + q);
-        dprev = dn;
+        for (int j = 0; j < L::kCols; ++j) Cprev[j] = u[j];
+        dprev = rhs;
         if (on && !failed) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) d.cprime[36 * n + 6 * r + c] = Crow[c];
-            d.dprime[6 * n + r] = dn;
+            for (int j = 0; j < L::kCols; ++j) d.cprime[36 * n + 6 * r + c0 + j] = u[j];
+            if (h == 0) d.dprime[6 * n + r] = rhs;
         }
     }
-    // Back substitution d_n = d'_n - C_n d_{n+1}, with the next node's C row
-    // and d' prefetched.
+    // Back substitution d_n = d'_n - C_n d_{n+1} (full C row in every lane).
     double next = 0.0;
     double pc[6], pd = 0.0;
     auto fetch_back = [&](uint32_t t) {
@@ -1411,33 +1421,29 @@ __device__ __forceinline__ void solve_group(const View &d, uint32_t warp)
         const bool coupled = on && t + 1 < len;
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
-            const double dq = __shfl_sync(FULL, next, base + q);  // every lane, every time: no divergent shuffles
-            if (coupled) value -= crow[q] * dq;
+            const double dq = __shfl_sync(FULL, next, base + q);
+            if (coupled) value = __fma_rn(-crow[q], dq, value);
         }
-        if (on) d.dir[6 * n + r] = value;
+        if (on && h == 0) d.dir[6 * n + r] = value;
         next = on ? value : 0.0;
     }
 }
 
-// Persistent warps pull strand groups from a queue, longest first, so the
-// long groups that bound the solve do not share a sub-partition's FP64 pipe
-// with a fixed share of the remaining work.
-__global__ void __launch_bounds__(128) k_block_solve(View d)
+template<int H> __global__ void __launch_bounds__(128) k_block_solve_aug(View d)
 {
-    const uint32_t groups = (d.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp;
+    const uint32_t groups = (d.S + AugLayout<H>::kStrands - 1) / AugLayout<H>::kStrands;
     for (;;) {
         uint32_t g = 0;
         if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
         g = __shfl_sync(0xffffffffu, g, 0);
         if (g >= groups) break;
-        solve_group(d, g);
+        solve_group_aug<H>(d, g);
     }
 }
 
-
 // ---- mixed form: float-float block solve with FP64 refinement -------------
 //
-// The same block Thomas recurrence as k_block_solve (per strand, one lane
+// The same block Thomas recurrence as the FP64 solve (per strand, one lane
 // per block row, Gauss-Jordan with partial pivoting on the first largest
 // |pivot|, relative diagonal shift) evaluated in float-float arithmetic:
 // k_ff_factor stores B_n^-1, C_n = B_n^-1 U_n and d'_n and writes the first
@@ -1450,7 +1456,7 @@ __global__ void __launch_bounds__(128) k_block_solve(View d)
 // (block condition numbers up to about 1e10); further sweeps run while the
 // largest relative correction of any strand exceeds kRefineRatio.  A pivot
 // below 1e-30 or a value outside the FP32 exponent range sets the solve
-// failure flag and the host falls back to k_block_solve.
+// failure flag and the host falls back to the FP64 block solve.
 
 constexpr float kRefineRatio = 1.0e-4f;
 constexpr int kRefineSweepsMax = 3;
@@ -2059,7 +2065,9 @@ struct Engine::Impl {
     struct KernelStat { const char *name; uint64_t launches; double ms; };
     bool profiling = false;
     uint64_t launches = 0;
-    unsigned solve_blocks = 0;  // launch shape of k_block_solve (0 = not tuned yet)
+    unsigned solve_blocks = 0;  // launch shape of the FP64 block solve (0 = not tuned yet)
+    void (*solve_kernel)(View) = nullptr;
+    unsigned ff_blocks = 0;     // launch shape of the float-float kernels
     std::vector<KernelStat> kstats;
     std::vector<std::pair<size_t, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     std::vector<cudaEvent_t> pool;
@@ -2517,44 +2525,72 @@ void Engine::make_steepest()
     limit_direction(I.mail_host->max_translation);
 }
 
-// Launch shape of the persistent block solve: 1, 2 or 3 blocks of four
-// warps per SM (or fewer when there are fewer strand groups), chosen once
-// by timing each on the first system.  The schedule does not change the
-// result: each strand group is solved by one warp in a fixed order.
+// Launch shape of the persistent FP64 block solve: the layout (H = 1: five
+// strands of 6 lanes per warp; H = 2: two strands of 12 lanes) and 1-4
+// blocks of four warps per SM, chosen once by timing each on the first
+// system.  The choice does not change the result: both layouts compute every
+// entry with the same operations, and each strand is solved by one group.
+KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm)
+{
+    Impl &I = *d_;
+    if (strands_per_warp == 0) { I.solve_blocks = 0; I.solve_kernel = nullptr; return KHS_OK; }
+    if ((strands_per_warp != 5 && strands_per_warp != 2) || blocks_per_sm < 1 || blocks_per_sm > 8)
+        return KHS_ERROR_INVALID_ARGUMENT;
+    int sms = 0;
+    KHS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, kDevice));
+    const unsigned groups = unsigned((I.v.S + strands_per_warp - 1) / strands_per_warp);
+    I.solve_kernel = strands_per_warp == 5 ? k_block_solve_aug<1> : k_block_solve_aug<2>;
+    I.solve_blocks = std::min(std::max(1u, (groups + 3) / 4), blocks_per_sm * unsigned(sms));
+    const unsigned ff_groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
+    I.ff_blocks = std::min(std::max(1u, (ff_groups + 3) / 4), 2u * unsigned(sms));
+    return KHS_OK;
+}
+
 void Engine::tune_block_solve()
 {
     Impl &I = *d_;
-    const unsigned groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
-    const unsigned most = std::max(1u, (groups + 3) / 4);
     int sms = 0;
     KHS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, kDevice));
-    unsigned best = std::min(most, unsigned(sms));
-    float best_ms = 3.0e38f;
     cudaEvent_t ev[2];
     KHS_CUDA(cudaEventCreate(&ev[0]));
     KHS_CUDA(cudaEventCreate(&ev[1]));
-    for (unsigned per_sm = 1; per_sm <= 3; ++per_sm) {
-        const unsigned blocks = std::min(most, per_sm * unsigned(sms));
-        float ms_min = 3.0e38f;
+    auto time_it = [&](void (*kernel)(View), unsigned blocks) {
+        float best = 3.0e38f;
         for (int rep = 0; rep < 2; ++rep) {
             KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
             KHS_CUDA(cudaEventRecord(ev[0], I.stream));
-            k_block_solve<<<blocks, 128, 0, I.stream>>>(I.v);
+            kernel<<<blocks, 128, 0, I.stream>>>(I.v);
             ++I.launches;
             KHS_CUDA(cudaEventRecord(ev[1], I.stream));
             KHS_CUDA(cudaEventSynchronize(ev[1]));
             float ms = 0.0f;
             KHS_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
-            ms_min = std::min(ms_min, ms);
+            best = std::min(best, ms);
         }
-        if (ms_min < best_ms) { best_ms = ms_min; best = blocks; }
-        if (blocks == most) break;
+        return best;
+    };
+    struct Candidate { void (*kernel)(View); unsigned strands_per_warp; };
+    const Candidate layouts[2] = {{k_block_solve_aug<1>, 5u}, {k_block_solve_aug<2>, 2u}};
+    float best_ms = 3.0e38f;
+    for (const Candidate &c : layouts) {
+        const unsigned groups = unsigned((I.v.S + c.strands_per_warp - 1) / c.strands_per_warp);
+        const unsigned most = std::max(1u, (groups + 3) / 4);
+        for (unsigned per_sm = 1; per_sm <= 4; ++per_sm) {
+            const unsigned blocks = std::min(most, per_sm * unsigned(sms));
+            const float ms = time_it(c.kernel, blocks);
+            if (ms < best_ms) { best_ms = ms; I.solve_kernel = c.kernel; I.solve_blocks = blocks; }
+            if (blocks == most) break;
+        }
+    }
+    // Float-float kernels (5 strands of 6 lanes per warp).
+    {
+        const unsigned groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
+        I.ff_blocks = std::min(std::max(1u, (groups + 3) / 4), 2u * unsigned(sms));
     }
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);
     KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
     KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_failed, 0, sizeof(int), I.stream));
-    I.solve_blocks = best;
 }
 
 bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
@@ -2565,11 +2601,11 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
     const Mailbox &mb = *I.mail_host;
     bool fp64 = mode_ != KHSX_MODE_MIXED_FF;
     if (!fp64) {
-        I.launch("k_ff_factor", k_ff_factor, I.solve_blocks, 128, I.v);
+        I.launch("k_ff_factor", k_ff_factor, I.ff_blocks, 128, I.v);
         uint32_t sweeps = 0;
         for (;;) {
             I.launch("k_ff_residual", k_ff_residual, grid_for(6 * size_t(I.v.N)), kBlock, I.v);
-            I.launch("k_ff_correct", k_ff_correct, I.solve_blocks, 128, I.v);
+            I.launch("k_ff_correct", k_ff_correct, I.ff_blocks, 128, I.v);
             ++sweeps;
             I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
             I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
@@ -2587,7 +2623,7 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
         }
     }
     if (fp64) {
-        I.launch("k_block_solve", k_block_solve, I.solve_blocks, 128, I.v);
+        I.launch("k_block_solve", I.solve_kernel, I.solve_blocks, 128, I.v);
         I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
         I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
         I.check();

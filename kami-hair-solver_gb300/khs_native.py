@@ -205,6 +205,7 @@ EXTENSION_FUNCTIONS = [
     ("khsxCopySubstepRecords", ctypes.c_int, [VP, P(SubstepRecord), c_u32]),
     ("khsxCopyContactRecords", ctypes.c_int, [VP, VP, c_u32]),
     ("khsxQueryContacts", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
+    ("khsxSetBlockSolveSchedule", ctypes.c_int, [VP, c_u32, c_u32]),
     ("khsxQueryContactsNoAlloc", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
     ("khsxSetProfiling", ctypes.c_int, [VP, c_u32]),
     ("khsxGetKernelTimings", c_u32, [VP, VP, c_u32]),
@@ -215,7 +216,7 @@ EXTENSION_FUNCTIONS = [
 
 # Entry points the CPU oracle does not provide (device-only measurement).
 DEVICE_ONLY = {"khsxSetProfiling", "khsxGetKernelTimings", "khsxResetKernelTimings", "khsxGetKernelLaunchCount",
-               "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc"}
+               "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc", "khsxSetBlockSolveSchedule"}
 
 # Size of the file-scope device scratch behind khsxQueryContactsNoAlloc
 # (KHSX_NO_ALLOC_SCRATCH_BYTES in the C header).
@@ -477,6 +478,9 @@ class HairSolver:
         out = np.zeros(count, dtype=CONTACT_DTYPE)
         self._check(self._library.khsxQueryContacts(self._handle, _ptr(q), q.size, _ptr(out), count))
         return out
+
+    def set_block_solve_schedule(self, strands_per_warp: int, blocks_per_sm: int = 1) -> None:
+        self._check(self._library.khsxSetBlockSolveSchedule(self._handle, strands_per_warp, blocks_per_sm))
 
     def query_contacts_no_alloc(self, q: np.ndarray, out: np.ndarray) -> int:
         """khsxQueryContactsNoAlloc into a caller-owned CONTACT_DTYPE array;

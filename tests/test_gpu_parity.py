@@ -161,3 +161,21 @@ def test_mixed_ff_sphere_moving(gpu_lib, oracle_lib):
     newton = sum(r.newton_iterations for fr in out for r in fr["records"])
     assert sum(r.fp64_fallbacks for fr in out for r in fr["records"]) == 0
     assert sweeps >= newton > 0
+
+
+def test_block_solve_layouts_bit_identical(gpu_lib):
+    """Every block-solve launch shape (5 strands of 6 lanes or 2 strands of
+    12 lanes per warp, any number of blocks per SM) gives bit-identical
+    trajectories, so the one-time launch tuning cannot change a result."""
+    sc = scenes.ellipsoid_scene(strands=200, frames=2)
+    finals = []
+    for spw, bps in ((5, 1), (2, 1), (2, 3), (5, 4)):
+        s = kn.HairSolver(gpu_lib)
+        scenes.load_into(s, sc)
+        s.set_block_solve_schedule(spw, bps)
+        for f in range(1, sc.frames):
+            assert s._library.khsStepAnimationFrame(s.handle, f, sc.frame_dt) == kn.OK, s.last_error()
+        finals.append(s.state())
+        s.close()
+    for q, v in finals[1:]:
+        assert np.array_equal(q, finals[0][0]) and np.array_equal(v, finals[0][1])
