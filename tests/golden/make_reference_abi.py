@@ -1,0 +1,27 @@
+"""Generates tests/golden/reference_abi.json from the reference project's
+public header (include/kami_hair_solver.h, ABI v5): every typedef'd struct
+with its field types, names and array lengths, every enum with its member
+values, and every exported function with its normalised signature.
+
+Run in a checkout that has the reference next to it:
+    python tests/golden/make_reference_abi.py /root/reference/include/kami_hair_solver.h
+"""
+import json
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+from abi_parse import parse_header  # noqa: E402
+
+
+def main() -> None:
+    src = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/include/kami_hair_solver.h")
+    abi = parse_header(src.read_text(encoding="utf-8"))
+    abi["source"] = "reference include/kami_hair_solver.h (ABI version 5)"
+    (HERE / "reference_abi.json").write_text(json.dumps(abi, indent=1, sort_keys=True) + "\n")
+    print(f"{len(abi['structs'])} structs, {len(abi['enums'])} enums, {len(abi['functions'])} functions")
+
+
+if __name__ == "__main__":
+    main()
