@@ -106,6 +106,7 @@ struct SweepRecord {
 struct View {
     uint32_t N, E, S, V, T, B;
     double *q, *q_old, *v, *q_base, *grad, *dir, *precond;
+    double *inertia;  // inertia + damping diagonal of each node's block [N][6]
     double *rot, *jl, *node_energy, *node_kinetic;
     double *diag, *upper, *cprime, *dprime;
     double *as_i_g, *as_j_g, *as_i_h, *as_j_h, *as_i_f, *as_j_f;
@@ -290,7 +291,7 @@ template<class F> __device__ void bvh_query_packed(const View &d, V lo, V hi, do
     bvh_positions_packed(d, lo, hi, pad, [&](uint32_t k) { f(d.border[k]); });
 }
 
-constexpr int kCacheLeaves = 16;
+constexpr int kCacheLeaves = 32;
 constexpr double kCacheSlack = 1.0e-3;  // metres each node may move before the cache is bypassed
 constexpr uint8_t kCacheInvalid = 0xff;
 
@@ -588,14 +589,13 @@ __global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int 
     if (gradient) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) d.jl[9 * size_t(n) + k] = J.m[k];
-        for (int k = 0; k < 36; ++k) d.diag[36 * size_t(n) + k] = 0.0;
     }
     if (d.fixed[n]) {
         d.node_energy[n] = 0.0;
         d.node_kinetic[n] = 0.0;
         if (gradient) {
 #pragma unroll
-            for (int k = 0; k < 6; ++k) d.grad[o + k] = 0.0;
+            for (int k = 0; k < 6; ++k) { d.grad[o + k] = 0.0; d.inertia[o + k] = 0.0; }
         }
         return;
     }
@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int 
         if (k < 3) kin += 0.5 * m * damp * damp * inv2;
         if (gradient) {
             d.grad[o + k] = kk * delta + c * damp;
-            d.diag[36 * size_t(n) + 7 * k] = kk + c;
+            d.inertia[o + k] = kk + c;
         }
     }
     d.node_energy[n] = obj;
@@ -1076,14 +1076,22 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_elem_eval(View 
 
 // Node sums in a fixed order: inertia, then the element on the left (this
 // node as its right end), then the element on the right.
+// One thread per entry (36 N diagonal-block entries, then 6 N gradient
+// entries) so every access is coalesced.  Diagonal block = inertia diagonal
+// + the contribution of the element whose right node is n + that of the
+// element whose left node is n, in that order.
 __global__ void __launch_bounds__(kBlock) k_node_sum(View d)
 {
-    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= d.N) return;
-    const size_t o6 = 6 * size_t(n), o36 = 36 * size_t(n);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) d.grad[o6 + k] = (d.grad[o6 + k] + d.as_j_g[o6 + k]) + d.as_i_g[o6 + k];
-    for (int k = 0; k < 36; ++k) d.diag[o36 + k] = (d.diag[o36 + k] + d.as_j_h[o36 + k]) + d.as_i_h[o36 + k];
+    const size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const size_t nh = 36 * size_t(d.N);
+    if (idx < nh) {
+        const size_t n = idx / 36, k = idx % 36;
+        const double base = (k % 7 == 0) ? d.inertia[6 * n + k / 7] : 0.0;
+        d.diag[idx] = (base + d.as_j_h[idx]) + d.as_i_h[idx];
+    } else if (idx < nh + 6 * size_t(d.N)) {
+        const size_t i = idx - nh;
+        d.grad[i] = (d.grad[i] + d.as_j_g[i]) + d.as_i_g[i];
+    }
 }
 
 // Block-level tree sum of one double per thread (blockDim == kBlock).
@@ -2157,7 +2165,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
                  B = m.bvh.size(), L = m.bvh.leaves.size(), O = m.mapping.size();
     // Arena sizing.
     size_t bytes = 0;
-    bytes += 12 * padded<double>(6 * N);     // q q_old v q_base grad dir precond dprime as_i_g as_j_g q_snap v_snap
+    bytes += 13 * padded<double>(6 * N);     // q q_old v q_base grad dir precond dprime as_i_g as_j_g q_snap v_snap inertia
     bytes += 5 * padded<double>(36 * N);     // diag upper cprime as_i_h as_j_h
     bytes += 2 * padded<double>(9 * N) + padded<double>(9 * N);  // rot jl ref
     bytes += 4 * padded<double>(N);          // node_energy kinetic mass rmass
@@ -2189,7 +2197,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.L = uint32_t(L);
     v.q = a.take<double>(6 * N); v.q_old = a.take<double>(6 * N); v.v = a.take<double>(6 * N);
     v.q_base = a.take<double>(6 * N); v.grad = a.take<double>(6 * N); v.dir = a.take<double>(6 * N);
-    v.precond = a.take<double>(6 * N); v.dprime = a.take<double>(6 * N);
+    v.precond = a.take<double>(6 * N); v.dprime = a.take<double>(6 * N); v.inertia = a.take<double>(6 * N);
     v.as_i_g = a.take<double>(6 * N); v.as_j_g = a.take<double>(6 * N);
     I.q_snap = a.take<double>(6 * N); I.v_snap = a.take<double>(6 * N);
     v.diag = a.take<double>(36 * N); v.upper = a.take<double>(36 * N); v.cprime = a.take<double>(36 * N);
@@ -2486,14 +2494,14 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
              trial ? 1 : 0, trial ? alpha : 0.0, dt);
     if (mode_ && v.has_collider) {
         const double *q = v.q;
-        I.launch("k_contact_filter", k_contact_filter, grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
+        I.launch(rebuild_cache_ ? "k_contact_filter_rebuild" : "k_contact_filter", k_contact_filter, grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
         I.launch("k_contact_exact", k_contact_exact, 152 * 4, kBlock, v, q);
         I.launch("k_contact_select", k_contact_select, grid_for(v.E), kBlock, v);
     }
     rebuild_cache_ = false;
     I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", mode_ ? k_elem_eval<true> : k_elem_eval<false>, grid_for(v.E),
              kBlock, v, gradient ? 1 : 0);
-    if (gradient) I.launch("k_node_sum", k_node_sum, grid_for(v.N), kBlock, v);
+    if (gradient) I.launch("k_node_sum", k_node_sum, grid_for(42 * size_t(v.N)), kBlock, v);
     I.launch("k_reduce_eval", k_reduce_eval, kPartials, kBlock, v, gradient ? 1 : 0);
     I.launch("k_final_eval", k_final_eval, 1, kBlock, v);
     I.check();
