@@ -414,6 +414,19 @@ KHS_API uint32_t khsxGetSolveMode(const KhsSolver *solver);
    directions.  Requires a built solver. */
 KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *solver, uint32_t strands_per_warp, uint32_t blocks_per_sm);
 
+/* Device-resident rollback ring: the rod state (q and v) after each of the
+   last `slots` successful animation frames stays in device memory (2 x 48
+   bytes per internal node per slot), so a serving loop can rewind a bake
+   without a host round trip.  slots 0 frees the ring.  Setting a ring also
+   stores the current frame.  Requires a built solver. */
+KHS_API KhsResult khsxSetRollbackRing(KhsSolver *solver, uint32_t slots);
+
+/* Restores q and v of `frame` from the ring (KHS_ERROR_INVALID_ARGUMENT if
+   the ring no longer holds it) and makes it the current animation frame;
+   later frames are dropped from the ring.  The next khsStepAnimationFrame
+   call steps frame + 1. */
+KHS_API KhsResult khsxRollbackToFrame(KhsSolver *solver, uint32_t frame);
+
 /* Copies the full generalised state: q and v are 6 * internal_node_count
    FP64 values each, per-node interleaved (x, y, z, rx, ry, rz).  Either
    pointer may be NULL. */

@@ -614,6 +614,26 @@ KHS_API KhsResult khsxSetSolveMode(KhsSolver *s, uint32_t mode)
 
 KHS_API uint32_t khsxGetSolveMode(const KhsSolver *s) { return s ? s->mode : 0; }
 
+KHS_API KhsResult khsxSetRollbackRing(KhsSolver *s, uint32_t slots)
+{
+    return guarded(s, [&] {
+        if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+        const KhsResult r = s->engine->set_rollback_ring(slots);
+        if (r != KHS_OK) s->error = s->engine->last_error();
+        return r;
+    });
+}
+
+KHS_API KhsResult khsxRollbackToFrame(KhsSolver *s, uint32_t frame)
+{
+    return guarded(s, [&] {
+        if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+        const KhsResult r = s->engine->rollback_to_frame(frame);
+        if (r != KHS_OK) s->error = s->engine->last_error();
+        return r;
+    });
+}
+
 KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *s, uint32_t strands_per_warp, uint32_t blocks_per_sm)
 {
     return guarded(s, [&] {

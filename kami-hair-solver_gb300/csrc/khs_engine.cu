@@ -2064,7 +2064,7 @@ struct Engine::Impl {
     double *root_cur_x = nullptr, *root_cur_r = nullptr, *root_pend_x = nullptr, *root_pend_r = nullptr;
     double *col_frame_start = nullptr, *col_pending = nullptr;
     double *anim_root_x = nullptr, *anim_root_r = nullptr, *anim_col = nullptr;
-    size_t anim_bytes = 0;
+    size_t anim_bytes = 0, ring_bytes = 0;
     double *col_a_copy = nullptr;  // frame-start copy used while stepping
     std::vector<uint8_t> fixed_host;
     uint64_t resident = 0;
@@ -2074,6 +2074,10 @@ struct Engine::Impl {
     bool profiling = false;
     uint64_t launches = 0;
     unsigned solve_blocks = 0;  // launch shape of the FP64 block solve (0 = not tuned yet)
+    // Rollback ring: q and v of the last ring_frame.size() animation frames,
+    // slot k holding frame ring_frame[k] (-1 = empty), [slots][2][N][6] FP64.
+    double *ring = nullptr;
+    std::vector<int64_t> ring_frame;
     void (*solve_kernel)(View) = nullptr;
     unsigned ff_blocks = 0;     // launch shape of the float-float kernels
     std::vector<KernelStat> kstats;
@@ -2129,6 +2133,7 @@ struct Engine::Impl {
         for (auto &p : pending) { pool.push_back(p.second.first); pool.push_back(p.second.second); }
         for (cudaEvent_t e : pool) cudaEventDestroy(e);
         if (arena.base) cudaFree(arena.base);
+        if (ring) cudaFree(ring);
         if (anim_root_x) cudaFree(anim_root_x);
         if (mail_host) cudaFreeHost(mail_host);
         if (sweep_host) cudaFreeHost(sweep_host);
@@ -2906,8 +2911,74 @@ KhsResult Engine::step_animation_frame(uint32_t frame, double frame_dt)
     const KhsResult r = run_frame(frame_dt, I.anim_root_x + a * N3, I.anim_root_r + a * N3, I.anim_root_x + b * N3,
                                   I.anim_root_r + b * N3, I.v.V ? I.anim_col + a * V3 : nullptr,
                                   I.v.V ? I.anim_col + b * V3 : nullptr, frame, animation_frames_);
-    if (r == KHS_OK) current_frame_ = frame;
+    if (r == KHS_OK) {
+        current_frame_ = frame;
+        push_ring(frame);
+    }
     return r;
+}
+
+void Engine::push_ring(uint32_t frame)
+{
+    Impl &I = *d_;
+    if (!I.ring) return;
+    const size_t slots = I.ring_frame.size(), qn = 6 * size_t(I.v.N);
+    const size_t k = frame % slots;
+    KHS_CUDA(cudaMemcpyAsync(I.ring + 2 * qn * k, I.v.q, qn * 8, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.ring + 2 * qn * k + qn, I.v.v, qn * 8, cudaMemcpyDeviceToDevice, I.stream));
+    I.ring_frame[k] = int64_t(frame);
+}
+
+KhsResult Engine::set_rollback_ring(uint32_t slots)
+{
+    Impl &I = *d_;
+    if (slots > 1024) return fail(KHS_ERROR_INVALID_ARGUMENT, "rollback ring holds at most 1024 frames");
+    I.sync();
+    if (I.ring) { cudaFree(I.ring); I.ring = nullptr; I.resident -= I.ring_bytes; I.ring_bytes = 0; }
+    I.ring_frame.clear();
+    if (!slots) return KHS_OK;
+    const size_t bytes = size_t(slots) * 2 * 6 * size_t(I.v.N) * 8;
+    if (cudaMalloc(reinterpret_cast<void **>(&I.ring), bytes) != cudaSuccess) {
+        I.ring = nullptr;
+        cudaGetLastError();
+        return fail(KHS_ERROR_OUT_OF_MEMORY, "cannot allocate the rollback ring");
+    }
+    I.ring_bytes = bytes;
+    I.resident += bytes;
+    I.ring_frame.assign(slots, -1);
+    gpu_stats_.resident_bytes = I.resident;
+    if (animation_ready_) push_ring(current_frame_);
+    return KHS_OK;
+}
+
+KhsResult Engine::rollback_to_frame(uint32_t frame)
+{
+    Impl &I = *d_;
+    if (!animation_ready_) return fail(KHS_ERROR_INVALID_STATE, "finalize the animation before rolling back");
+    const size_t slots = I.ring_frame.size();
+    if (!I.ring || !slots || I.ring_frame[frame % slots] != int64_t(frame))
+        return fail(KHS_ERROR_INVALID_ARGUMENT, "frame is not held by the rollback ring");
+    const size_t qn = 6 * size_t(I.v.N), k = frame % slots, qb = qn * 8;
+    KHS_CUDA(cudaMemcpyAsync(I.v.q, I.ring + 2 * qn * k, qb, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.v.v, I.ring + 2 * qn * k + qn, qb, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.v.q_old, I.v.q, qb, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.q_snap, I.v.q, qb, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.v_snap, I.v.v, qb, cudaMemcpyDeviceToDevice, I.stream));
+    I.sync();
+    // Frames after the restored one are no longer on this trajectory.
+    for (size_t j = 0; j < slots; ++j)
+        if (I.ring_frame[j] > int64_t(frame)) I.ring_frame[j] = -1;
+    current_frame_ = frame;
+    cancel_.store(false);
+    progress_frame_.store(frame);
+    progress_substep_.store(0); progress_substep_count_.store(0); progress_iteration_.store(0);
+    progress_phase_.store(KHS_PHASE_FINISHED);
+    step_stats_ = {};
+    step_stats_.struct_size = sizeof(step_stats_);
+    step_stats_.phase = KHS_PHASE_FINISHED;
+    clear_failure();
+    error_.clear();
+    return KHS_OK;
 }
 
 namespace {

@@ -56,6 +56,10 @@ public:
     uint64_t checkpoint_size() const;
     KhsResult save_checkpoint(void *data, uint64_t capacity);
     KhsResult restore_checkpoint(const void *data, uint64_t size);
+    // Device-resident rollback ring of the last `slots` animation frames
+    // (q and v), filled after every successful animation frame.
+    KhsResult set_rollback_ring(uint32_t slots);
+    KhsResult rollback_to_frame(uint32_t frame);
 
     KhsResult copy_original_positions(KhsVec3 *out, uint32_t capacity) const;
     KhsResult copy_internal_positions(KhsVec3 *out, uint32_t capacity) const;
@@ -104,6 +108,7 @@ private:
     EvalStats evaluate(bool gradient, double dt, double alpha_for_trial);
     bool make_direction(KhsxSubstepRecord &rec, double grad_norm2);
     void tune_block_solve();
+    void push_ring(uint32_t frame);
     void make_steepest();
     void limit_direction(double max_translation);
 

@@ -206,6 +206,8 @@ EXTENSION_FUNCTIONS = [
     ("khsxCopyContactRecords", ctypes.c_int, [VP, VP, c_u32]),
     ("khsxQueryContacts", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
     ("khsxSetBlockSolveSchedule", ctypes.c_int, [VP, c_u32, c_u32]),
+    ("khsxSetRollbackRing", ctypes.c_int, [VP, c_u32]),
+    ("khsxRollbackToFrame", ctypes.c_int, [VP, c_u32]),
     ("khsxQueryContactsNoAlloc", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
     ("khsxSetProfiling", ctypes.c_int, [VP, c_u32]),
     ("khsxGetKernelTimings", c_u32, [VP, VP, c_u32]),
@@ -216,7 +218,8 @@ EXTENSION_FUNCTIONS = [
 
 # Entry points the CPU oracle does not provide (device-only measurement).
 DEVICE_ONLY = {"khsxSetProfiling", "khsxGetKernelTimings", "khsxResetKernelTimings", "khsxGetKernelLaunchCount",
-               "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc", "khsxSetBlockSolveSchedule"}
+               "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc", "khsxSetBlockSolveSchedule",
+               "khsxSetRollbackRing", "khsxRollbackToFrame"}
 
 # Size of the file-scope device scratch behind khsxQueryContactsNoAlloc
 # (KHSX_NO_ALLOC_SCRATCH_BYTES in the C header).
@@ -478,6 +481,12 @@ class HairSolver:
         out = np.zeros(count, dtype=CONTACT_DTYPE)
         self._check(self._library.khsxQueryContacts(self._handle, _ptr(q), q.size, _ptr(out), count))
         return out
+
+    def set_rollback_ring(self, slots: int) -> None:
+        self._check(self._library.khsxSetRollbackRing(self._handle, slots))
+
+    def rollback_to_frame(self, frame: int) -> None:
+        self._check(self._library.khsxRollbackToFrame(self._handle, frame))
 
     def set_block_solve_schedule(self, strands_per_warp: int, blocks_per_sm: int = 1) -> None:
         self._check(self._library.khsxSetBlockSolveSchedule(self._handle, strands_per_warp, blocks_per_sm))

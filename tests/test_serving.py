@@ -1,0 +1,42 @@
+"""Serving loop host logic on CPU with the oracle library: requests are
+admitted by slot and byte budget (never exceeding either), every request
+completes, and each result equals the same request run alone."""
+import numpy as np
+
+import khs_native as kn
+import scenes
+import serving
+
+
+def _stream(n, seed=9):
+    reqs = []
+    for i in range(n):
+        sc = scenes.sphere_scene(seed=seed + i, strands=6 + 2 * i, nodes=8, frames=2, motion=True)
+        reqs.append(serving.Request(rid=i, scene=sc, arrival=0.01 * i, frames=2))
+    return reqs
+
+
+def test_admission_respects_budget_and_results_match_solo(oracle_lib):
+    oracle_lib.lib.khsOracleSetThreads(1)
+    reqs = _stream(5)
+    sizes = [serving.estimate_bytes(r.scene, 0) for r in reqs]
+    budget = max(sizes) + min(sizes)  # at most two requests fit at once
+    server = serving.Server(oracle_lib, budget, max_slots=3, mode=kn.MODE_PLAIN_FP64, ring_slots=0)
+    mixed = server.run(reqs)
+    assert server.peak_bytes <= budget and server.peak_slots <= 3
+    assert all(r.status == kn.OK for r in mixed), [r.error for r in mixed]
+    for req, res in zip(reqs, mixed):
+        solo = serving.run_request(oracle_lib, req, kn.MODE_PLAIN_FP64, 0)
+        assert np.array_equal(solo.q, res.q)
+        assert len(res.frame_ms) == req.frames
+    s = serving.summary(mixed, server.makespan)
+    assert s["completed"] == len(reqs) and s["p99_frame_ms"] >= s["p50_frame_ms"] > 0
+
+
+def test_request_over_budget_is_rejected(oracle_lib):
+    reqs = _stream(2)
+    server = serving.Server(oracle_lib, serving.estimate_bytes(reqs[0].scene, 0), max_slots=2,
+                            mode=kn.MODE_PLAIN_FP64, ring_slots=0)
+    res = server.run(reqs)
+    assert res[0].status == kn.OK
+    assert res[1].status == kn.ERROR_INVALID_ARGUMENT and "budget" in res[1].error
