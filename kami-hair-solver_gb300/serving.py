@@ -87,7 +87,7 @@ def run_request(lib, req: Request, mode: int, ring_slots: int) -> Result:
     try:
         scenes.load_into(s, req.scene, frames=req.frames + 1)
         s.set_solve_mode(mode)
-        if ring_slots and hasattr(s._library.lib, "khsxSetRollbackRing"):
+        if ring_slots and hasattr(s._library, "khsxSetRollbackRing"):
             s.set_rollback_ring(ring_slots)
         res.nodes = int(s.build_stats().internal_node_count)
         for f in range(1, req.frames + 1):
