@@ -276,20 +276,25 @@ def time_frames(lib, scene, mode: int, args, torch, flush, world: int) -> dict:
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     clock_info = clocks.stop()
+    import replicas
+
     out = {"device_s": sum(frame_ms) / 1e3, "wall_s": wall, "substeps": substeps, "newton": newton,
            "candidates": candidates, "frame_ms": frame_ms, "clocks": clock_info,
            "launches": solver.kernel_launches() - launches0, "timings": solver.kernel_timings(),
-           "stats": solver.build_stats()}
+           "stats": solver.build_stats(), "checksum": replicas.state_checksum(solver.state()[0])}
     solver.set_profiling(False)
     solver.close()
     return out
 
 
-def _max_over_ranks(torch, world: int, x: float) -> float:
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+def _aggregate(run: dict, world: int) -> dict:
+    """Replicas: SUM of substeps over ranks / MAX of device seconds."""
+    import replicas
+
+    dist = None
     if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    return float(t.item())
+        import torch.distributed as dist
+    return replicas.aggregate(run["substeps"], run["device_s"], run["checksum"], dist, "cuda")
 
 
 def _roofline(run: dict, fp64_peak: float) -> dict:
@@ -340,17 +345,19 @@ def run_ours(args) -> None:
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     modes = {"plain": kn.MODE_PLAIN_FP64, "mixed": kn.MODE_MIXED}
     main = time_frames(lib, scene, modes[args.mode], args, torch, flush, world)
-    device_s = _max_over_ranks(torch, world, main["device_s"])
-    value = world * main["substeps"] / device_s
+    agg = _aggregate(main, world)
+    device_s, value = agg["max_seconds"], agg["value"]
     plain = None
     if args.mode == "mixed" and not args.skip_plain:
         ref = time_frames(lib, scene, kn.MODE_PLAIN_FP64, args, torch, flush, world)
-        plain_s = _max_over_ranks(torch, world, ref["device_s"])
-        plain = {"value": world * ref["substeps"] / plain_s, "unit": UNIT, "ms_per_step": 1e3 * plain_s / args.steps,
+        ragg = _aggregate(ref, world)
+        plain_s = ragg["max_seconds"]
+        plain = {"value": ragg["value"], "unit": UNIT, "ms_per_step": 1e3 * plain_s / args.steps,
                  "substeps": ref["substeps"], "newton_iterations": ref["newton"], "speedup_of_mixed": None,
                  "top_kernels": dict(list(_roofline(ref, fp64_peak.value)["kernel_shares"].items())[:4])}
         plain["speedup_of_mixed"] = value / plain["value"]
         plain["same_iterates"] = ref["substeps"] == main["substeps"] and ref["newton"] == main["newton"]
+        plain["same_final_state"] = ref["checksum"] == main["checksum"]
 
     # End to end through the public API with host buffers.
     e2e = run_e2e(lib, scene, args, torch) if not args.skip_e2e else None
@@ -368,7 +375,7 @@ def run_ours(args) -> None:
             "plain_fp64": plain, "clocks": main["clocks"], "gpu_launches": int(main["launches"]),
             "wall_s": main["wall_s"], "substeps": main["substeps"], "newton_iterations": main["newton"],
             "frame_ms": [round(x, 2) for x in main["frame_ms"]], "fp64_pipe_peak_tflops": fp64_peak.value,
-            "fp32_pipe_peak_tflops": fp32_peak.value,
+            "fp32_pipe_peak_tflops": fp32_peak.value, "replica_checksums": agg["checksums"],
         }
         print(json.dumps(line), flush=True)
     if world > 1:
