@@ -262,29 +262,56 @@ KHS_HD void xtdy(const M &X, const double d[3], const M &Y, double *out, int ld,
 
 // Gauss-Newton Hessian blocks L0 J^T diag(w) J of one element, as 6x6
 // row-major blocks: Hii, Hjj (diagonal blocks of the two nodes) and Hij
-// (rows of node i, columns of node j).
+// (rows of node i, columns of node j).  With the strain Jacobian's
+// structure (shear/stretch rows -A, Sgi, A, Sgj; curvature rows 0, Kki, 0,
+// Kkj) the blocks reduce to six 3x3 products:
+//   P = A^T Wg A, Xi = A^T Wg Sgi, Xj = A^T Wg Sgj,
+//   Rii = Sgi^T Wg Sgi + Kki^T Wk Kki, Rjj likewise, Rij = Sgi^T Wg Sgj + Kki^T Wk Kkj,
+//   Hii = [P, -Xi; -Xi^T, Rii], Hjj = [P, Xj; Xj^T, Rjj], Hij = [-P, -Xj; Xi^T, Rij],
+// with the symmetric ones (P, Rii, Rjj) evaluated on one triangle and mirrored.
+KHS_HD double dot3w(const M &X, int r, const M &WY, int c)
+{
+    return X.m[r] * WY.m[c] + X.m[3 + r] * WY.m[3 + c] + X.m[6 + r] * WY.m[6 + c];
+}
+
 KHS_HD void element_hessian(const ElementJacobian &J, const Weights &w, double L0, double *Hii, double *Hjj, double *Hij)
 {
-    const double dg[3] = {L0 * w.w[0], L0 * w.w[1], L0 * w.w[2]};
-    const double dk[3] = {L0 * w.w[3], L0 * w.w[4], L0 * w.w[5]};
-    // translation-translation: A^T Wg A (with signs -,+ for i,j)
-    xtdy(J.A, dg, J.A, Hii, 6, false, 1.0);
-    xtdy(J.A, dg, J.A, Hjj, 6, false, 1.0);
-    xtdy(J.A, dg, J.A, Hij, 6, false, -1.0);
-    // translation-rotation
-    xtdy(J.A, dg, J.Sgi, Hii + 3, 6, false, -1.0);   // xi,ui
-    xtdy(J.Sgi, dg, J.A, Hii + 18, 6, false, -1.0);  // ui,xi
-    xtdy(J.A, dg, J.Sgj, Hjj + 3, 6, false, 1.0);    // xj,uj
-    xtdy(J.Sgj, dg, J.A, Hjj + 18, 6, false, 1.0);   // uj,xj
-    xtdy(J.A, dg, J.Sgj, Hij + 3, 6, false, -1.0);   // xi,uj
-    xtdy(J.Sgi, dg, J.A, Hij + 18, 6, false, 1.0);   // ui,xj
-    // rotation-rotation
-    xtdy(J.Sgi, dg, J.Sgi, Hii + 21, 6, false, 1.0);
-    xtdy(J.Kki, dk, J.Kki, Hii + 21, 6, true, 1.0);
-    xtdy(J.Sgj, dg, J.Sgj, Hjj + 21, 6, false, 1.0);
-    xtdy(J.Kkj, dk, J.Kkj, Hjj + 21, 6, true, 1.0);
-    xtdy(J.Sgi, dg, J.Sgj, Hij + 21, 6, false, 1.0);
-    xtdy(J.Kki, dk, J.Kkj, Hij + 21, 6, true, 1.0);
+    M WA, WSi, WSj, WKi, WKj;  // rows scaled by L0 w
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double g = L0 * w.w[k], kk = L0 * w.w[3 + k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            WA.m[3 * k + c] = g * J.A.m[3 * k + c];
+            WSi.m[3 * k + c] = g * J.Sgi.m[3 * k + c];
+            WSj.m[3 * k + c] = g * J.Sgj.m[3 * k + c];
+            WKi.m[3 * k + c] = kk * J.Kki.m[3 * k + c];
+            WKj.m[3 * k + c] = kk * J.Kkj.m[3 * k + c];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double xi = dot3w(J.A, r, WSi, c), xj = dot3w(J.A, r, WSj, c);
+            Hii[6 * r + 3 + c] = -xi;
+            Hii[6 * (3 + c) + r] = -xi;
+            Hjj[6 * r + 3 + c] = xj;
+            Hjj[6 * (3 + c) + r] = xj;
+            Hij[6 * r + 3 + c] = -xj;
+            Hij[6 * (3 + c) + r] = xi;
+            Hij[6 * (3 + r) + 3 + c] = dot3w(J.Sgi, r, WSj, c) + dot3w(J.Kki, r, WKj, c);
+            if (c < r) continue;
+            const double p = dot3w(J.A, r, WA, c);
+            const double rii = dot3w(J.Sgi, r, WSi, c) + dot3w(J.Kki, r, WKi, c);
+            const double rjj = dot3w(J.Sgj, r, WSj, c) + dot3w(J.Kkj, r, WKj, c);
+            Hii[6 * r + c] = p; Hii[6 * c + r] = p;
+            Hjj[6 * r + c] = p; Hjj[6 * c + r] = p;
+            Hij[6 * r + c] = -p; Hij[6 * c + r] = -p;
+            Hii[6 * (3 + r) + 3 + c] = rii; Hii[6 * (3 + c) + 3 + r] = rii;
+            Hjj[6 * (3 + r) + 3 + c] = rjj; Hjj[6 * (3 + c) + 3 + r] = rjj;
+        }
+    }
 }
 
 // ---- geometry (device flavour, cuda_backend.cu:200-223) ----------------

@@ -874,14 +874,8 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
         }
         d.c_cand[e] = cand;
         if (n > uint32_t(kSurvivors)) {
-            // Rare: more near-equal candidates than slots; finish in place.
-            uint32_t c2 = 0;
-            dm::ClosestPair pair;
-            const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
-            const uint32_t closest =
-                inside ? closest_triangle_in(d, xi, xj, c2, pair, [&](auto &&fn) { leaves_query(d, leaves, nl, lo, hi, pad, fn); })
-                       : closest_triangle<true>(d, xi, xj, pad, c2, pair);
-            write_contact(d, e, closest, pair);
+            // Rare: more near-equal candidates than slots; k_contact_select
+            // finishes the element with the in-thread search.
             d.surv_n[e] = kSurvOverflow;
         } else {
             d.surv_n[e] = uint8_t(n);
@@ -923,13 +917,35 @@ __global__ void __launch_bounds__(kBlock) k_contact_exact(View d, const double *
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_contact_select(View d)
+__global__ void __launch_bounds__(kBlock) k_contact_select(View d, const double *q)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e == 0) d.sc->surv_count = 0;  // k_contact_exact, its only reader, has completed
     if (e >= d.E) return;
     const uint32_t n = d.surv_n[e];
-    if (n == 0 || n == kSurvOverflow) return;
+    if (n == 0) return;
+    if (n == kSurvOverflow) {
+        // The two-pass search over the same candidates (the cached leaves
+        // when the filter used them, else the full walk).
+        const uint32_t i = d.ei[e], j = d.ej[e];
+        const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
+        const double pad = d.radius + d.offset + d.dhat;
+        const uint8_t nl = d.cache_n[e];
+        const double *cx = d.cache_x + 6 * size_t(e);
+        const V ci = load3(cx), cj = load3(cx + 3);
+        const bool inside = nl != kCacheInvalid && fabs(xi.x - ci.x) <= kCacheSlack && fabs(xi.y - ci.y) <= kCacheSlack &&
+                            fabs(xi.z - ci.z) <= kCacheSlack && fabs(xj.x - cj.x) <= kCacheSlack &&
+                            fabs(xj.y - cj.y) <= kCacheSlack && fabs(xj.z - cj.z) <= kCacheSlack;
+        const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
+        const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
+        uint32_t c2 = 0;
+        dm::ClosestPair pair;
+        const uint32_t closest =
+            inside ? closest_triangle_in(d, xi, xj, c2, pair, [&](auto &&fn) { leaves_query(d, leaves, nl, lo, hi, pad, fn); })
+                   : closest_triangle<true>(d, xi, xj, pad, c2, pair);
+        write_contact(d, e, closest, pair);
+        return;
+    }
     uint32_t best = 0;
     double bd = 1.0e300;
     for (uint32_t k = 0; k < n; ++k) {
@@ -1264,7 +1280,7 @@ constexpr int kSolveGroup = 6, kSolveGroupsPerWarp = 5;  // float-float kernels:
 // owns one strand: lane (r, h) holds row r, columns [6h/H, 6(h+1)/H) of B_n
 // and U_n; every lane of row r holds rhs_n[r].  H = 1 puts 5 strands in a
 // warp, H = 2 puts 2 strands in a warp and halves the instructions on each
-// strand's sequential chain.  Every entry is computed by the same sequence
+// strand's sequential chain, H = 3 gives one strand 18 lanes.  Every entry is computed by the same sequence
 // of operations in both layouts, so the results are identical bit for bit
 // and the launch tuner may pick either.
 template<int H> struct AugLayout {
@@ -2501,7 +2517,7 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
         const double *q = v.q;
         I.launch(rebuild_cache_ ? "k_contact_filter_rebuild" : "k_contact_filter", k_contact_filter, grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
         I.launch("k_contact_exact", k_contact_exact, 152 * 4, kBlock, v, q);
-        I.launch("k_contact_select", k_contact_select, grid_for(v.E), kBlock, v);
+        I.launch("k_contact_select", k_contact_select, grid_for(v.E), kBlock, v, q);
     }
     rebuild_cache_ = false;
     I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", mode_ ? k_elem_eval<true> : k_elem_eval<false>, grid_for(v.E),
@@ -2539,7 +2555,8 @@ void Engine::make_steepest()
 }
 
 // Launch shape of the persistent FP64 block solve: the layout (H = 1: five
-// strands of 6 lanes per warp; H = 2: two strands of 12 lanes) and 1-4
+// strands of 6 lanes per warp; H = 2: two strands of 12 lanes; H = 3: one
+// strand of 18 lanes) and 1-4
 // blocks of four warps per SM, chosen once by timing each on the first
 // system.  The choice does not change the result: both layouts compute every
 // entry with the same operations, and each strand is solved by one group.
@@ -2547,12 +2564,12 @@ KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t b
 {
     Impl &I = *d_;
     if (strands_per_warp == 0) { I.solve_blocks = 0; I.solve_kernel = nullptr; return KHS_OK; }
-    if ((strands_per_warp != 5 && strands_per_warp != 2) || blocks_per_sm < 1 || blocks_per_sm > 8)
+    if ((strands_per_warp != 5 && strands_per_warp != 2 && strands_per_warp != 1) || blocks_per_sm < 1 || blocks_per_sm > 8)
         return KHS_ERROR_INVALID_ARGUMENT;
     int sms = 0;
     KHS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, kDevice));
     const unsigned groups = unsigned((I.v.S + strands_per_warp - 1) / strands_per_warp);
-    I.solve_kernel = strands_per_warp == 5 ? k_block_solve_aug<1> : k_block_solve_aug<2>;
+    I.solve_kernel = strands_per_warp == 5 ? k_block_solve_aug<1> : strands_per_warp == 2 ? k_block_solve_aug<2> : k_block_solve_aug<3>;
     I.solve_blocks = std::min(std::max(1u, (groups + 3) / 4), blocks_per_sm * unsigned(sms));
     const unsigned ff_groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
     I.ff_blocks = std::min(std::max(1u, (ff_groups + 3) / 4), 2u * unsigned(sms));
@@ -2583,7 +2600,7 @@ void Engine::tune_block_solve()
         return best;
     };
     struct Candidate { void (*kernel)(View); unsigned strands_per_warp; };
-    const Candidate layouts[2] = {{k_block_solve_aug<1>, 5u}, {k_block_solve_aug<2>, 2u}};
+    const Candidate layouts[3] = {{k_block_solve_aug<1>, 5u}, {k_block_solve_aug<2>, 2u}, {k_block_solve_aug<3>, 1u}};
     float best_ms = 3.0e38f;
     for (const Candidate &c : layouts) {
         const unsigned groups = unsigned((I.v.S + c.strands_per_warp - 1) / c.strands_per_warp);

@@ -73,7 +73,7 @@ public:
     KhsResult query_contacts_no_alloc(const double *q, uint64_t dof, KhsxContactRecord *out, uint32_t capacity);
 
     void set_mode(uint32_t mode) { mode_ = mode; }
-    // Block-solve launch shape: 5 or 2 strands per warp and blocks of four
+    // Block-solve launch shape: 5, 2 or 1 strands per warp and blocks of four
     // warps per SM; 0 strands per warp restores the one-time tuning.
     KhsResult set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm);
     uint32_t mode() const { return mode_; }

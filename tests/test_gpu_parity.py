@@ -164,12 +164,12 @@ def test_mixed_ff_sphere_moving(gpu_lib, oracle_lib):
 
 
 def test_block_solve_layouts_bit_identical(gpu_lib):
-    """Every block-solve launch shape (5 strands of 6 lanes or 2 strands of
-    12 lanes per warp, any number of blocks per SM) gives bit-identical
+    """Every block-solve launch shape (5 strands of 6 lanes, 2 of 12 or 1 of
+    18 lanes per warp, any number of blocks per SM) gives bit-identical
     trajectories, so the one-time launch tuning cannot change a result."""
     sc = scenes.ellipsoid_scene(strands=200, frames=2)
     finals = []
-    for spw, bps in ((5, 1), (2, 1), (2, 3), (5, 4)):
+    for spw, bps in ((5, 1), (2, 1), (2, 3), (5, 4), (1, 1)):
         s = kn.HairSolver(gpu_lib)
         scenes.load_into(s, sc)
         s.set_block_solve_schedule(spw, bps)
