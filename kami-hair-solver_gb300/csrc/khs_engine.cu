@@ -107,6 +107,7 @@ struct View {
     uint32_t N, E, S, V, T, B;
     double *q, *q_old, *v, *q_base, *grad, *dir, *precond;
     double *inertia;  // inertia + damping diagonal of each node's block [N][6]
+    float *q32;       // FP32 copy of the node positions [N][3] (mixed contact filter)
     double *rot, *jl, *node_energy, *node_kinetic;
     double *diag, *upper, *cprime, *dprime;
     double *as_i_g, *as_j_g, *as_i_h, *as_j_h, *as_i_f, *as_j_f;
@@ -138,6 +139,7 @@ struct View {
     uint32_t *cache_leaf;
     uint8_t *cache_n;
     double *cache_x;
+    float *cache_x32;  // FP32 copy of cache_x for the filter's slack test
     // Mixed contact pass in three launches: FP32 vertex records of every
     // triangle in leaf order (a, b, c as three float4, the triangle index in
     // the first .w), the survivors of the FP32 filter per element (at most
@@ -247,6 +249,34 @@ __device__ __forceinline__ QueryBox make_query(V lo, V hi, double pad)
     return qb;
 }
 
+// The same box from FP32 copies of the segment's end points (lo32, hi32 =
+// componentwise min / max of the rounded coordinates): rounding to nearest
+// moved each coordinate by at most 2^-24 of its magnitude, so widening by
+// 2^-23 of the magnitude (plus 1e-30) bounds the FP64 box from outside and
+// narrowing by the same bounds it from inside.  lo and hi (FP64) serve the
+// exact leaf test.
+__device__ __forceinline__ QueryBox make_query_f(const float lo32[3], const float hi32[3], V lo, V hi, double pad)
+{
+    QueryBox qb;
+    qb.lo = lo; qb.hi = hi; qb.pad = pad;
+    const float k = 1.1920929e-7f;  // 2^-23
+    qb.olx = __fsub_rd(lo32[0], __fmaf_ru(fabsf(lo32[0]), k, 1e-30f));
+    qb.oly = __fsub_rd(lo32[1], __fmaf_ru(fabsf(lo32[1]), k, 1e-30f));
+    qb.olz = __fsub_rd(lo32[2], __fmaf_ru(fabsf(lo32[2]), k, 1e-30f));
+    qb.ohx = __fadd_ru(hi32[0], __fmaf_ru(fabsf(hi32[0]), k, 1e-30f));
+    qb.ohy = __fadd_ru(hi32[1], __fmaf_ru(fabsf(hi32[1]), k, 1e-30f));
+    qb.ohz = __fadd_ru(hi32[2], __fmaf_ru(fabsf(hi32[2]), k, 1e-30f));
+    qb.ilx = __fadd_ru(lo32[0], __fmaf_ru(fabsf(lo32[0]), k, 1e-30f));
+    qb.ily = __fadd_ru(lo32[1], __fmaf_ru(fabsf(lo32[1]), k, 1e-30f));
+    qb.ilz = __fadd_ru(lo32[2], __fmaf_ru(fabsf(lo32[2]), k, 1e-30f));
+    qb.ihx = __fsub_rd(hi32[0], __fmaf_ru(fabsf(hi32[0]), k, 1e-30f));
+    qb.ihy = __fsub_rd(hi32[1], __fmaf_ru(fabsf(hi32[1]), k, 1e-30f));
+    qb.ihz = __fsub_rd(hi32[2], __fmaf_ru(fabsf(hi32[2]), k, 1e-30f));
+    qb.opad = __double2float_ru(pad);
+    qb.ipad = __double2float_rd(pad);
+    return qb;
+}
+
 __device__ __forceinline__ bool maybe_overlap(const QueryBox &q, float4 a, float4 b)
 {
     return q.olx <= __fadd_ru(b.x, q.opad) && a.x <= __fadd_ru(q.ohx, q.opad) && q.oly <= __fadd_ru(b.y, q.opad) &&
@@ -269,9 +299,8 @@ __device__ __forceinline__ bool leaf_overlap_exact(const View &d, uint32_t node,
 // visited node (box + escape, box + leaf range (first << 4 | count)).
 // f receives the position of each candidate in leaf order (index into
 // border and tri32).
-template<class F> __device__ void bvh_positions_packed(const View &d, V lo, V hi, double pad, F &&f)
+template<class F> __device__ void bvh_positions_packed(const View &d, const QueryBox &q, F &&f)
 {
-    const QueryBox q = make_query(lo, hi, pad);
     uint32_t i = 0;
     while (i < d.B) {
         const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
@@ -288,7 +317,7 @@ template<class F> __device__ void bvh_positions_packed(const View &d, V lo, V hi
 
 template<class F> __device__ void bvh_query_packed(const View &d, V lo, V hi, double pad, F &&f)
 {
-    bvh_positions_packed(d, lo, hi, pad, [&](uint32_t k) { f(d.border[k]); });
+    bvh_positions_packed(d, make_query(lo, hi, pad), [&](uint32_t k) { f(d.border[k]); });
 }
 
 constexpr int kCacheLeaves = 32;
@@ -318,10 +347,9 @@ __device__ uint32_t collect_leaves(const View &d, V lo, V hi, double pad, uint32
 // per-leaf test: the same candidates in the same order as the full walk,
 // provided the list holds every leaf that test can accept.  f receives
 // leaf-order positions.
-template<class F> __device__ void leaves_positions(const View &d, const uint32_t *leaves, uint32_t n, V lo, V hi, double pad,
+template<class F> __device__ void leaves_positions(const View &d, const uint32_t *leaves, uint32_t n, const QueryBox &q,
                                                    F &&f)
 {
-    const QueryBox q = make_query(lo, hi, pad);
     for (uint32_t k = 0; k < n; ++k) {
         const uint32_t i = leaves[k];
         const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
@@ -333,7 +361,7 @@ template<class F> __device__ void leaves_positions(const View &d, const uint32_t
 
 template<class F> __device__ void leaves_query(const View &d, const uint32_t *leaves, uint32_t n, V lo, V hi, double pad, F &&f)
 {
-    leaves_positions(d, leaves, n, lo, hi, pad, [&](uint32_t k) { f(d.border[k]); });
+    leaves_positions(d, leaves, n, make_query(lo, hi, pad), [&](uint32_t k) { f(d.border[k]); });
 }
 
 template<bool MIXED, class F> __device__ __forceinline__ void bvh_walk(const View &d, V lo, V hi, double pad, F &&f)
@@ -582,6 +610,7 @@ __global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int 
 #pragma unroll
         for (int k = 0; k < 6; ++k) q[k] = d.q[o + k];
     }
+    d.q32[3 * size_t(n)] = float(q[0]); d.q32[3 * size_t(n) + 1] = float(q[1]); d.q32[3 * size_t(n) + 2] = float(q[2]);
     M R, J;
     dm::rotation_and_jacobian(dm::v(q[3], q[4], q[5]), d.ref + 9 * size_t(n), R, gradient ? &J : nullptr);
 #pragma unroll
@@ -789,10 +818,11 @@ __device__ __forceinline__ float record_distance_f(const View &d, uint32_t p, dm
 // Filter of one element over a position source; returns the survivor count
 // (kSurvivors + 1 or more on overflow; the first kSurvivors are stored).
 template<class Source>
-__device__ __forceinline__ uint32_t filter_survivors(const View &d, uint32_t e, V xi, V xj, uint32_t &cand, Source &&source)
+__device__ __forceinline__ uint32_t filter_survivors(const View &d, uint32_t e, dm::F3 xi32, dm::F3 xj32, uint32_t &cand,
+                                                     Source &&source)
 {
-    const dm::F3 origin = dm::f3(float(xi.x), float(xi.y), float(xi.z));
-    const dm::F3 p0 = dm::f3(0.f, 0.f, 0.f), p1 = dm::f3(float(xj.x) - origin.x, float(xj.y) - origin.y, float(xj.z) - origin.z);
+    const dm::F3 origin = xi32;
+    const dm::F3 p0 = dm::f3(0.f, 0.f, 0.f), p1 = dm::f3(xj32.x - origin.x, xj32.y - origin.y, xj32.z - origin.z);
     float bound = 3.0e38f;
     cand = 0;
     source([&](uint32_t p) {
@@ -834,6 +864,18 @@ __device__ __forceinline__ void write_contact(const View &d, uint32_t e, uint32_
     store3(d.c_bary + 3 * size_t(e), pair.bary);
 }
 
+// Slack test of the leaf cache on the FP32 copies: the copies differ from
+// the FP64 positions by at most 2^-24 of a coordinate's magnitude, so the
+// margin of 1e-5 m keeps every accepted displacement within kCacheSlack
+// for coordinates below a few hundred metres.
+__device__ __forceinline__ bool within_cache_slack(const float *c, dm::F3 xi, dm::F3 xj)
+{
+    const float s = float(kCacheSlack) - 1.0e-5f;
+    return fabsf(xi.x - c[0]) <= s && fabsf(xi.y - c[1]) <= s && fabsf(xi.z - c[2]) <= s && fabsf(xj.x - c[3]) <= s &&
+           fabsf(xj.y - c[4]) <= s && fabsf(xj.z - c[5]) <= s;
+}
+
+// q must be d.q (its FP32 copy d.q32 is read).
 __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double *q, int cache)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -842,35 +884,30 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
     if (live) {
         const uint32_t i = d.ei[e], j = d.ej[e];
         uint32_t cand = 0, n = 0;
-        V xi = dm::v(0, 0, 0), xj = xi;
         const bool enabled = d.has_collider && !d.fixed[i] && d.econtact[e];
-        bool inside = false;
-        uint8_t nl = 0;
-        const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
-        const double pad = d.radius + d.offset + d.dhat;
         if (enabled) {
-            xi = load3(q + 6 * size_t(i)); xj = load3(q + 6 * size_t(j));
-            if (cache >= 0) {
-                double *cx = d.cache_x + 6 * size_t(e);
-                if (cache == 1) {
-                    const V s3 = dm::v(kCacheSlack, kCacheSlack, kCacheSlack);
-                    uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
-                    const uint32_t c = collect_leaves(d, dm::vmin(xi, xj) - s3, dm::vmax(xi, xj) + s3, pad, slots, kCacheLeaves);
-                    d.cache_n[e] = c <= uint32_t(kCacheLeaves) ? uint8_t(c) : kCacheInvalid;
-                    store3(cx, xi);
-                    store3(cx + 3, xj);
-                }
-                nl = d.cache_n[e];
-                const V ci = load3(cx), cj = load3(cx + 3);
-                inside = nl != kCacheInvalid && fabs(xi.x - ci.x) <= kCacheSlack && fabs(xi.y - ci.y) <= kCacheSlack &&
-                         fabs(xi.z - ci.z) <= kCacheSlack && fabs(xj.x - cj.x) <= kCacheSlack &&
-                         fabs(xj.y - cj.y) <= kCacheSlack && fabs(xj.z - cj.z) <= kCacheSlack;
+            const dm::F3 xi32 = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
+            const dm::F3 xj32 = dm::f3(d.q32[3 * size_t(j)], d.q32[3 * size_t(j) + 1], d.q32[3 * size_t(j) + 2]);
+            const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
+            const double pad = d.radius + d.offset + d.dhat;
+            const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
+            float *c32 = d.cache_x32 + 6 * size_t(e);
+            if (cache == 1) {
+                const V s3 = dm::v(kCacheSlack, kCacheSlack, kCacheSlack);
+                uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
+                const uint32_t c = collect_leaves(d, dm::vmin(xi, xj) - s3, dm::vmax(xi, xj) + s3, pad, slots, kCacheLeaves);
+                d.cache_n[e] = c <= uint32_t(kCacheLeaves) ? uint8_t(c) : kCacheInvalid;
+                c32[0] = xi32.x; c32[1] = xi32.y; c32[2] = xi32.z; c32[3] = xj32.x; c32[4] = xj32.y; c32[5] = xj32.z;
             }
-            const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
+            const uint8_t nl = cache >= 0 ? d.cache_n[e] : kCacheInvalid;
+            const bool inside = nl != kCacheInvalid && within_cache_slack(c32, xi32, xj32);
+            const float lo32[3] = {fminf(xi32.x, xj32.x), fminf(xi32.y, xj32.y), fminf(xi32.z, xj32.z)};
+            const float hi32[3] = {fmaxf(xi32.x, xj32.x), fmaxf(xi32.y, xj32.y), fmaxf(xi32.z, xj32.z)};
+            const QueryBox qb = make_query_f(lo32, hi32, dm::vmin(xi, xj), dm::vmax(xi, xj), pad);
             if (inside)
-                n = filter_survivors(d, e, xi, xj, cand, [&](auto &&fn) { leaves_positions(d, leaves, nl, lo, hi, pad, fn); });
+                n = filter_survivors(d, e, xi32, xj32, cand, [&](auto &&fn) { leaves_positions(d, leaves, nl, qb, fn); });
             else
-                n = filter_survivors(d, e, xi, xj, cand, [&](auto &&fn) { bvh_positions_packed(d, lo, hi, pad, fn); });
+                n = filter_survivors(d, e, xi32, xj32, cand, [&](auto &&fn) { bvh_positions_packed(d, qb, fn); });
         }
         d.c_cand[e] = cand;
         if (n > uint32_t(kSurvivors)) {
@@ -931,11 +968,9 @@ __global__ void __launch_bounds__(kBlock) k_contact_select(View d, const double 
         const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
         const double pad = d.radius + d.offset + d.dhat;
         const uint8_t nl = d.cache_n[e];
-        const double *cx = d.cache_x + 6 * size_t(e);
-        const V ci = load3(cx), cj = load3(cx + 3);
-        const bool inside = nl != kCacheInvalid && fabs(xi.x - ci.x) <= kCacheSlack && fabs(xi.y - ci.y) <= kCacheSlack &&
-                            fabs(xi.z - ci.z) <= kCacheSlack && fabs(xj.x - cj.x) <= kCacheSlack &&
-                            fabs(xj.y - cj.y) <= kCacheSlack && fabs(xj.z - cj.z) <= kCacheSlack;
+        const dm::F3 xi32 = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
+        const dm::F3 xj32 = dm::f3(d.q32[3 * size_t(j)], d.q32[3 * size_t(j) + 1], d.q32[3 * size_t(j) + 2]);
+        const bool inside = nl != kCacheInvalid && within_cache_slack(d.cache_x32 + 6 * size_t(e), xi32, xj32);
         const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
         const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
         uint32_t c2 = 0;
@@ -1336,19 +1371,13 @@ template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, u
         for (int q = 0; q < 6; ++q) ucol[q] = nuc[q];
         if (t + 1 < maxlen) fetch(t + 1);
         if (t > 0) {
-            // B -= U_{n-1}^T C_{n-1}, rhs -= U_{n-1}^T d'_{n-1}
-            double sum[L::kCols], sr = 0.0;
-#pragma unroll
-            for (int j = 0; j < L::kCols; ++j) sum[j] = 0.0;
+            // B = D - U_{n-1}^T C_{n-1}, rhs = -g - U_{n-1}^T d'_{n-1}
 #pragma unroll
             for (int q = 0; q < 6; ++q) {
 #pragma unroll
-                for (int j = 0; j < L::kCols; ++j) sum[j] = __fma_rn(ucol[q], __shfl_sync(FULL, Cprev[j], base + 6 * h + q), sum[j]);
-                sr = __fma_rn(ucol[q], __shfl_sync(FULL, dprev, base + q), sr);
+                for (int j = 0; j < L::kCols; ++j) a[j] = __fma_rn(-ucol[q], __shfl_sync(FULL, Cprev[j], base + 6 * h + q), a[j]);
+                rhs = __fma_rn(-ucol[q], __shfl_sync(FULL, dprev, base + q), rhs);
             }
-#pragma unroll
-            for (int j = 0; j < L::kCols; ++j) a[j] = __dsub_rn(a[j], sum[j]);
-            rhs = __dsub_rn(rhs, sr);
         }
         // Relative diagonal shift max(1e-12 max|b_ii|, 1e-24).
         double diag_r = 0.0;
@@ -1364,7 +1393,12 @@ template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, u
         const double shift = fmax(__dmul_rn(1.0e-12, __longlong_as_double((long long)smax)), 1.0e-24);
 #pragma unroll
         for (int j = 0; j < L::kCols; ++j) if (c0 + j == r) a[j] = __dadd_rn(a[j], shift);
+        // Gauss-Jordan with the pivot rows left unscaled: row r is divided
+        // by its pivot (the value at column r when it became the pivot row)
+        // once at the end, so each column costs one reciprocal, one product
+        // and one fused multiply-add per live entry.
         bool ok = true;
+        double ipiv = 1.0;
 #pragma unroll
         for (int col = 0; col < 6; ++col) {
             const int hc = col / L::kCols, jc = col % L::kCols;
@@ -1394,22 +1428,26 @@ template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, u
 #pragma unroll
             for (int j = 0; j < L::kCols; ++j) if (j == jc && h == hc) acol = a[j];
             const double ip = __drcp_rn(__shfl_sync(FULL, acol, owner_half + col));
-            const double f = __shfl_sync(FULL, acol, owner_half + r);
+            const double fp = __dmul_rn(__shfl_sync(FULL, acol, owner_half + r), ip);
+            if (r == col) ipiv = ip;
             const int prow = base + 6 * h + col;
 #pragma unroll
             for (int j = 0; j < L::kCols; ++j) {
-                if (H == 1 && j <= col) continue;  // finished columns (H = 1: known at compile time)
-                const double p = __dmul_rn(__shfl_sync(FULL, a[j], prow), ip);
-                a[j] = (r == col) ? p : __fma_rn(-f, p, a[j]);
+                if (L::kCols * (H - 1) + j <= col) continue;  // finished in every lane
+                const double x = __shfl_sync(FULL, a[j], prow);
+                a[j] = (r == col) ? a[j] : __fma_rn(-fp, x, a[j]);
             }
 #pragma unroll
             for (int j = 0; j < L::kCols; ++j) {
-                const double p = __dmul_rn(__shfl_sync(FULL, u[j], prow), ip);
-                u[j] = (r == col) ? p : __fma_rn(-f, p, u[j]);
+                const double x = __shfl_sync(FULL, u[j], prow);
+                u[j] = (r == col) ? u[j] : __fma_rn(-fp, x, u[j]);
             }
-            const double pr = __dmul_rn(__shfl_sync(FULL, rhs, prow), ip);
-            rhs = (r == col) ? pr : __fma_rn(-f, pr, rhs);
+            const double xr = __shfl_sync(FULL, rhs, prow);
+            rhs = (r == col) ? rhs : __fma_rn(-fp, xr, rhs);
         }
+#pragma unroll
+        for (int j = 0; j < L::kCols; ++j) u[j] = __dmul_rn(u[j], ipiv);
+        rhs = __dmul_rn(rhs, ipiv);
         if (on && !ok) {
             failed = true;
             if (gl == 0) atomicExch(&d.sc->solve_failed, 1);
@@ -2201,6 +2239,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     const size_t pair_capacity = std::min<size_t>(std::max<size_t>(size_t(1) << 20, 8 * E), size_t(16) << 20);
     bytes += 2 * padded<double>(E) + padded<double>(3 * E) + 2 * padded<uint32_t>(pair_capacity);
     bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E) + padded<double>(6 * E);
+    bytes += padded<float>(3 * N) + padded<float>(6 * E);
     bytes += 2 * padded<float2>(36 * N) + padded<float2>(6 * N) + padded<float>(N);
     bytes += padded<float4>(3 * T) + 2 * padded<uint32_t>(size_t(kSurvivors) * E) + padded<uint8_t>(E) +
              padded<double>(5 * size_t(kSurvivors) * E);
@@ -2219,6 +2258,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.q = a.take<double>(6 * N); v.q_old = a.take<double>(6 * N); v.v = a.take<double>(6 * N);
     v.q_base = a.take<double>(6 * N); v.grad = a.take<double>(6 * N); v.dir = a.take<double>(6 * N);
     v.precond = a.take<double>(6 * N); v.dprime = a.take<double>(6 * N); v.inertia = a.take<double>(6 * N);
+    v.q32 = a.take<float>(3 * N);
     v.as_i_g = a.take<double>(6 * N); v.as_j_g = a.take<double>(6 * N);
     I.q_snap = a.take<double>(6 * N); I.v_snap = a.take<double>(6 * N);
     v.diag = a.take<double>(36 * N); v.upper = a.take<double>(36 * N); v.cprime = a.take<double>(36 * N);
@@ -2249,6 +2289,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.pair_elem = a.take<uint32_t>(pair_capacity); v.pair_tri = a.take<uint32_t>(pair_capacity);
     v.pair_capacity = uint32_t(pair_capacity);
     v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E); v.cache_x = a.take<double>(6 * E);
+    v.cache_x32 = a.take<float>(6 * E);
     v.tri32 = a.take<float4>(3 * T);
     v.ff_inv = a.take<float2>(36 * N); v.ff_c = a.take<float2>(36 * N); v.ff_d = a.take<float2>(6 * N);
     v.ff_shift = a.take<float>(N);
