@@ -892,15 +892,21 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
             const double pad = d.radius + d.offset + d.dhat;
             const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
             float *c32 = d.cache_x32 + 6 * size_t(e);
-            if (cache == 1) {
+            uint8_t nl = cache >= 0 ? d.cache_n[e] : kCacheInvalid;
+            bool inside = cache == 0 && nl != kCacheInvalid && within_cache_slack(c32, xi32, xj32);
+            if (cache == 1 || (cache == 0 && !inside)) {
+                // (Re)collect the leaves around the element box grown by the
+                // slack: one walk, after which both filter passes read the
+                // short leaf list (an element that left its slack would
+                // otherwise walk the tree twice in every evaluation).
                 const V s3 = dm::v(kCacheSlack, kCacheSlack, kCacheSlack);
                 uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
                 const uint32_t c = collect_leaves(d, dm::vmin(xi, xj) - s3, dm::vmax(xi, xj) + s3, pad, slots, kCacheLeaves);
-                d.cache_n[e] = c <= uint32_t(kCacheLeaves) ? uint8_t(c) : kCacheInvalid;
+                nl = c <= uint32_t(kCacheLeaves) ? uint8_t(c) : kCacheInvalid;
+                d.cache_n[e] = nl;
                 c32[0] = xi32.x; c32[1] = xi32.y; c32[2] = xi32.z; c32[3] = xj32.x; c32[4] = xj32.y; c32[5] = xj32.z;
+                inside = nl != kCacheInvalid;
             }
-            const uint8_t nl = cache >= 0 ? d.cache_n[e] : kCacheInvalid;
-            const bool inside = nl != kCacheInvalid && within_cache_slack(c32, xi32, xj32);
             const float lo32[3] = {fminf(xi32.x, xj32.x), fminf(xi32.y, xj32.y), fminf(xi32.z, xj32.z)};
             const float hi32[3] = {fmaxf(xi32.x, xj32.x), fmaxf(xi32.y, xj32.y), fmaxf(xi32.z, xj32.z)};
             const QueryBox qb = make_query_f(lo32, hi32, dm::vmin(xi, xj), dm::vmax(xi, xj), pad);
@@ -1939,6 +1945,14 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_ccd(View d)
 // stops a pair once 0.9 alpha reaches the global minimum found so far (every
 // limit the pair could still produce is >= 0.9 alpha).  The minimum equals
 // the per-element kernel's.
+// Candidates of the swept element box (positions at step 0 and 1) whose
+// FP32 lower-bound distance does not rule out a limit below 1: a pair is
+// skipped only when even the lower bound of 0.8 (dist - target) reaches the
+// speed, so the first advancement step of the exact pass would leave the
+// step unlimited anyway.  When all four swept end points stay within the
+// slack of the element's leaf cache, the cached leaves (collected with the
+// contact padding, which is at least the CCD target) hold every leaf the
+// swept box can touch and replace the tree walk.
 __global__ void __launch_bounds__(kBlock) k_ccd_collect(View d)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1949,18 +1963,35 @@ __global__ void __launch_bounds__(kBlock) k_ccd_collect(View d)
     const V d0 = load3(d.dir + 6 * size_t(i)), d1 = load3(d.dir + 6 * size_t(j));
     const double speed = fmax(dm::gnorm(d0), dm::gnorm(d1));
     if (speed < 1e-30) return;
-    const V lo = dm::vmin(dm::vmin(p0, p1), dm::vmin(p0 + d0, p1 + d1));
-    const V hi = dm::vmax(dm::vmax(p0, p1), dm::vmax(p0 + d0, p1 + d1));
+    const V e0 = p0 + d0, e1 = p1 + d1;
+    const V lo = dm::vmin(dm::vmin(p0, p1), dm::vmin(e0, e1));
+    const V hi = dm::vmax(dm::vmax(p0, p1), dm::vmax(e0, e1));
     const double target = d.radius + d.offset + d.min_gap;
-    const dm::F3 origin = dm::f3(float(p0.x), float(p0.y), float(p0.z));
-    const dm::F3 f0 = dm::f3(0.f, 0.f, 0.f), f1 = dm::f3(float(p1.x) - origin.x, float(p1.y) - origin.y, float(p1.z) - origin.z);
-    bvh_query_packed(d, lo, hi, target, [&](uint32_t t) {
+    const dm::F3 origin = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
+    const dm::F3 f0 = dm::f3(0.f, 0.f, 0.f);
+    const dm::F3 f1 = dm::f3(d.q32[3 * size_t(j)] - origin.x, d.q32[3 * size_t(j) + 1] - origin.y,
+                             d.q32[3 * size_t(j) + 2] - origin.z);
+    const float target_ru = __double2float_ru(target);
+    const float speed_ru = __fmul_ru(__double2float_ru(speed), 1.000002f);
+    const QueryBox qb = make_query(lo, hi, target);
+    auto test = [&](uint32_t p) {
         float m;
-        const float df = candidate_distance_f(d, t, origin, f0, f1, m);
-        if (0.8 * (double(df) - double(m) - target) >= speed * (1.0 + 1e-6)) return;
+        uint32_t t;
+        const float df = record_distance_f(d, p, origin, f0, f1, m, t);
+        if (__fmul_rd(0.8f, __fsub_rd(__fsub_rd(df, m), target_ru)) >= speed_ru) return;
         const uint32_t slot = atomicAdd(&d.sc->pair_count, 1u);
         if (slot < d.pair_capacity) { d.pair_elem[slot] = e; d.pair_tri[slot] = t; }
-    });
+    };
+    const uint8_t nl = d.cache_n[e];
+    bool cached = nl != kCacheInvalid && d.dhat >= d.min_gap;
+    if (cached) {
+        const float *c = d.cache_x32 + 6 * size_t(e);
+        const dm::F3 xj32 = dm::f3(d.q32[3 * size_t(j)], d.q32[3 * size_t(j) + 1], d.q32[3 * size_t(j) + 2]);
+        const dm::F3 a0 = dm::f3(float(e0.x), float(e0.y), float(e0.z)), a1 = dm::f3(float(e1.x), float(e1.y), float(e1.z));
+        cached = within_cache_slack(c, origin, xj32) && within_cache_slack(c, a0, a1);
+    }
+    if (cached) leaves_positions(d, d.cache_leaf + size_t(kCacheLeaves) * e, nl, qb, test);
+    else bvh_positions_packed(d, qb, test);
 }
 
 __global__ void __launch_bounds__(kBlock) k_ccd_pairs(View d)
