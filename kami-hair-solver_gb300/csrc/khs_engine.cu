@@ -83,6 +83,8 @@ struct Scalars {
     uint32_t surv_count;  // entries of the mixed contact pass's FP64 work list
     uint32_t solve_next;  // next strand group of the block-solve work queue
     uint32_t refine_bits; // largest relative refinement correction (FP32 bits)
+    uint32_t near_count;  // elements queued for the warp-cooperative contact pass
+    uint32_t pad;
 };
 
 struct Partial {
@@ -151,6 +153,7 @@ struct View {
     float2 *ff_inv, *ff_c, *ff_d;
     float *ff_shift;
     uint32_t *surv_tri, *surv_list;
+    uint32_t *near_list;  // elements with cached leaves, one warp each in k_contact_near
     uint8_t *surv_n;
     double *surv_res;
     const uint32_t *besc, *bfirst, *bcount, *border, *bleaves;
@@ -780,6 +783,7 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact(View d,
 // tie-break included, equals k_contact's and the all-FP64 search.
 
 constexpr int kSurvivors = 8;
+constexpr int kLeafTriangles = 8;  // BVH leaves hold at most 8 triangles (cuda_backend.cu:305)
 constexpr uint8_t kSurvOverflow = 0xff;
 
 // FP32 vertex records of every triangle in leaf order; run whenever col_cur
@@ -884,6 +888,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
     if (live) {
         const uint32_t i = d.ei[e], j = d.ej[e];
         uint32_t cand = 0, n = 0;
+        bool deferred = false;  // finished by k_contact_near
         const bool enabled = d.has_collider && !d.fixed[i] && d.econtact[e];
         if (enabled) {
             const dm::F3 xi32 = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
@@ -910,23 +915,30 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
             const float lo32[3] = {fminf(xi32.x, xj32.x), fminf(xi32.y, xj32.y), fminf(xi32.z, xj32.z)};
             const float hi32[3] = {fmaxf(xi32.x, xj32.x), fmaxf(xi32.y, xj32.y), fmaxf(xi32.z, xj32.z)};
             const QueryBox qb = make_query_f(lo32, hi32, dm::vmin(xi, xj), dm::vmax(xi, xj), pad);
-            if (inside)
-                n = filter_survivors(d, e, xi32, xj32, cand, [&](auto &&fn) { leaves_positions(d, leaves, nl, qb, fn); });
-            else
+            if (inside) {
+                if (nl > 0) {
+                    // k_contact_near finishes the element, one warp over its leaves.
+                    d.near_list[atomicAdd(&d.sc->near_count, 1u)] = e;
+                    deferred = true;
+                }
+            } else {
                 n = filter_survivors(d, e, xi32, xj32, cand, [&](auto &&fn) { bvh_positions_packed(d, qb, fn); });
+            }
         }
-        d.c_cand[e] = cand;
-        if (n > uint32_t(kSurvivors)) {
-            // Rare: more near-equal candidates than slots; k_contact_select
-            // finishes the element with the in-thread search.
-            d.surv_n[e] = kSurvOverflow;
-        } else {
-            d.surv_n[e] = uint8_t(n);
-            append = n;
-            if (n == 0) {
-                dm::ClosestPair pair;
-                pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
-                write_contact(d, e, kNone, pair);
+        if (!deferred) {
+            d.c_cand[e] = cand;
+            if (n > uint32_t(kSurvivors)) {
+                // Rare: more near-equal candidates than slots; k_contact_select
+                // finishes the element with the in-thread search.
+                d.surv_n[e] = kSurvOverflow;
+            } else {
+                d.surv_n[e] = uint8_t(n);
+                append = n;
+                if (n == 0) {
+                    dm::ClosestPair pair;
+                    pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
+                    write_contact(d, e, kNone, pair);
+                }
             }
         }
     }
@@ -947,6 +959,105 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
     for (uint32_t k = 0; k < append; ++k) d.surv_list[start + k] = uint32_t(kSurvivors) * e + k;
 }
 
+// One warp per element with cached leaves: lane l tests cached leaf l
+// (DFS order) and evaluates the FP32 distances of that leaf's triangles, so
+// the element's candidates are examined in parallel instead of one after
+// another by a single lane.  The candidate order is leaf order, then
+// triangle order within the leaf, as in the single-lane filter; survivors
+// are compacted in that order (a prefix over lanes, then ascending within a
+// lane), so slots, the FP64 pass and the ordered selection are unchanged.
+__global__ void __launch_bounds__(kBlock) k_contact_near(View d)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t count = d.sc->near_count;
+    const double pad = d.radius + d.offset + d.dhat;
+    for (uint32_t k = warp; k < count; k += nwarps) {
+        const uint32_t e = d.near_list[k];
+        const uint32_t i = d.ei[e], j = d.ej[e];
+        const dm::F3 xi32 = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
+        const dm::F3 xj32 = dm::f3(d.q32[3 * size_t(j)], d.q32[3 * size_t(j) + 1], d.q32[3 * size_t(j) + 2]);
+        const V xi = load3(d.q + 6 * size_t(i)), xj = load3(d.q + 6 * size_t(j));
+        const float lo32[3] = {fminf(xi32.x, xj32.x), fminf(xi32.y, xj32.y), fminf(xi32.z, xj32.z)};
+        const float hi32[3] = {fmaxf(xi32.x, xj32.x), fmaxf(xi32.y, xj32.y), fmaxf(xi32.z, xj32.z)};
+        const QueryBox qb = make_query_f(lo32, hi32, dm::vmin(xi, xj), dm::vmax(xi, xj), pad);
+        const uint32_t nl = d.cache_n[e];
+        uint32_t first = 0, cnt = 0;
+        if (uint32_t(lane) < nl) {
+            const uint32_t node = d.cache_leaf[size_t(kCacheLeaves) * e + lane];
+            const float4 a = __ldg(d.bnode + 2 * size_t(node)), b = __ldg(d.bnode + 2 * size_t(node) + 1);
+            if (maybe_overlap(qb, a, b) && leaf_overlap_exact(d, node, a, b, qb)) {
+                const uint32_t leaf = __float_as_uint(b.w);
+                first = leaf >> 4;
+                cnt = leaf & 15u;
+            }
+        }
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        const dm::F3 origin = xi32, p0 = dm::f3(0.f, 0.f, 0.f);
+        const dm::F3 p1 = dm::f3(xj32.x - origin.x, xj32.y - origin.y, xj32.z - origin.z);
+        float lb[kLeafTriangles];
+        uint32_t tri[kLeafTriangles];
+        float ub = 3.0e38f;
+#pragma unroll
+        for (int r = 0; r < kLeafTriangles; ++r) {
+            lb[r] = 3.0e38f;
+            tri[r] = 0;
+            if (uint32_t(r) < cnt) {
+                float m;
+                const float df = record_distance_f(d, first + r, origin, p0, p1, m, tri[r]);
+                lb[r] = df - m;
+                ub = fminf(ub, df + m);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ub = fminf(ub, __shfl_xor_sync(FULL, ub, o));
+        uint32_t mine = 0;
+#pragma unroll
+        for (int r = 0; r < kLeafTriangles; ++r) mine += (uint32_t(r) < cnt && !(lb[r] > ub)) ? 1u : 0u;
+        uint32_t sincl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(FULL, sincl, o);
+            if (lane >= o) sincl += v;
+        }
+        const uint32_t n = __shfl_sync(FULL, sincl, 31);
+        uint32_t slot = sincl - mine;
+        uint32_t *slots = d.surv_tri + size_t(kSurvivors) * e;
+#pragma unroll
+        for (int r = 0; r < kLeafTriangles; ++r) {
+            if (uint32_t(r) < cnt && !(lb[r] > ub)) {
+                if (slot < uint32_t(kSurvivors)) slots[slot] = tri[r];
+                ++slot;
+            }
+        }
+        uint32_t base = 0;
+        if (lane == 0) {
+            d.c_cand[e] = total;
+            if (n > uint32_t(kSurvivors)) {
+                d.surv_n[e] = kSurvOverflow;
+            } else {
+                d.surv_n[e] = uint8_t(n);
+                if (n == 0) {
+                    dm::ClosestPair pair;
+                    pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
+                    write_contact(d, e, kNone, pair);
+                } else {
+                    base = atomicAdd(&d.sc->surv_count, n);
+                }
+            }
+        }
+        base = __shfl_sync(FULL, base, 0);
+        if (n <= uint32_t(kSurvivors) && uint32_t(lane) < n) d.surv_list[base + lane] = uint32_t(kSurvivors) * e + lane;
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_contact_exact(View d, const double *q)
 {
     const uint32_t count = d.sc->surv_count;
@@ -963,7 +1074,10 @@ __global__ void __launch_bounds__(kBlock) k_contact_exact(View d, const double *
 __global__ void __launch_bounds__(kBlock) k_contact_select(View d, const double *q)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e == 0) d.sc->surv_count = 0;  // k_contact_exact, its only reader, has completed
+    if (e == 0) {  // k_contact_near and k_contact_exact, their only readers, have completed
+        d.sc->surv_count = 0;
+        d.sc->near_count = 0;
+    }
     if (e >= d.E) return;
     const uint32_t n = d.surv_n[e];
     if (n == 0) return;
@@ -2103,6 +2217,7 @@ __global__ void k_init_scalars(View d)
     d.sc->surv_count = 0;
     d.sc->solve_next = 0;
     d.sc->refine_bits = 0;
+    d.sc->near_count = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -2271,6 +2386,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     bytes += 2 * padded<double>(E) + padded<double>(3 * E) + 2 * padded<uint32_t>(pair_capacity);
     bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E) + padded<double>(6 * E);
     bytes += padded<float>(3 * N) + padded<float>(6 * E);
+    bytes += padded<uint32_t>(E);
     bytes += 2 * padded<float2>(36 * N) + padded<float2>(6 * N) + padded<float>(N);
     bytes += padded<float4>(3 * T) + 2 * padded<uint32_t>(size_t(kSurvivors) * E) + padded<uint8_t>(E) +
              padded<double>(5 * size_t(kSurvivors) * E);
@@ -2326,6 +2442,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.ff_shift = a.take<float>(N);
     v.surv_tri = a.take<uint32_t>(size_t(kSurvivors) * E); v.surv_list = a.take<uint32_t>(size_t(kSurvivors) * E);
     v.surv_n = a.take<uint8_t>(E); v.surv_res = a.take<double>(5 * size_t(kSurvivors) * E);
+    v.near_list = a.take<uint32_t>(E);
     if (E) KHS_CUDA(cudaMemsetAsync(v.cache_n, kCacheInvalid, E, I.stream));
     uint32_t *besc = a.take<uint32_t>(B), *bfirst = a.take<uint32_t>(B), *bcount = a.take<uint32_t>(B);
     v.brefit = a.take<uint32_t>(B);
@@ -2588,6 +2705,7 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
     if (mode_ && v.has_collider) {
         const double *q = v.q;
         I.launch(rebuild_cache_ ? "k_contact_filter_rebuild" : "k_contact_filter", k_contact_filter, grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
+        I.launch("k_contact_near", k_contact_near, 152 * 8, kBlock, v);
         I.launch("k_contact_exact", k_contact_exact, 152 * 4, kBlock, v, q);
         I.launch("k_contact_select", k_contact_select, grid_for(v.E), kBlock, v, q);
     }
