@@ -175,29 +175,34 @@ def _oracle_library():
     return lib
 
 
-def cpu_oracle_sample(scene, warm_frames: int, sample_frames: int, substeps: int, threads: int | None = None) -> dict:
+def cpu_oracle_sample(scene, full_frames: int, repeats: int, substeps: int, threads: int | None = None) -> dict:
     """Times the CPU oracle on a bounded sample of the workload: frames
-    1..warm_frames run in full (untimed), then each of the next sample_frames
-    frames is cut after its first ``substeps`` substeps (timed)."""
+    1..full_frames run in full (untimed) and are checkpointed; each of
+    ``repeats`` timed samples restores that checkpoint and runs the first
+    ``substeps`` substeps of frame full_frames + 1."""
     import khs_native as kn
     import scenes
 
     lib = _oracle_library()
     cores = int(lib.lib.khsOracleSetThreads(threads or os.cpu_count() or 1))
     s = kn.HairSolver(lib)
-    scenes.load_into(s, scene, frames=warm_frames + sample_frames + 1)
+    scenes.load_into(s, scene, frames=full_frames + 2)
     lib.lib.khsOracleSetSubstepLimit(0)
-    for f in range(1, warm_frames + 1):
-        s._library.khsStepAnimationFrame(s.handle, f, scene.frame_dt)
-    lib.lib.khsOracleSetSubstepLimit(substeps)
-    done, newton, seconds, per_step = 0, 0, 0.0, []
-    for f in range(warm_frames + 1, warm_frames + sample_frames + 1):
-        t0 = time.perf_counter()
+    for f in range(1, full_frames + 1):
         r = s._library.khsStepAnimationFrame(s.handle, f, scene.frame_dt)
-        dt = time.perf_counter() - t0
-        st = s.stats()
         if r != kn.OK:
             raise RuntimeError(f"oracle frame {f} failed ({r}): {s.last_error()}")
+    checkpoint = s.save_checkpoint()
+    lib.lib.khsOracleSetSubstepLimit(substeps)
+    done, newton, seconds, per_step = 0, 0, 0.0, []
+    for _ in range(repeats):
+        s.restore_checkpoint(checkpoint)
+        t0 = time.perf_counter()
+        r = s._library.khsStepAnimationFrame(s.handle, full_frames + 1, scene.frame_dt)
+        dt = time.perf_counter() - t0
+        if r != kn.OK:
+            raise RuntimeError(f"oracle frame {full_frames + 1} failed ({r}): {s.last_error()}")
+        st = s.stats()
         done += st.converged_substeps
         newton += st.newton_iterations
         seconds += dt
@@ -206,8 +211,9 @@ def cpu_oracle_sample(scene, warm_frames: int, sample_frames: int, substeps: int
     lib.lib.khsOracleSetSubstepLimit(0)
     return {"value": done / seconds, "unit": UNIT, "cores": cores, "kind": "port", "seconds": seconds,
             "substeps": done, "newton_iterations": newton, "per_step_s": per_step,
-            "sample": f"first {substeps} substeps of frames {warm_frames + 1}-{warm_frames + sample_frames} of the same "
-                      f"body scene after frames 1-{warm_frames} in full (untimed); CPU FP64 oracle on {cores} threads"}
+            "sample": f"first {substeps} substeps of frame {full_frames + 1} of the same body scene ({repeats} "
+                      f"run(s) from a checkpoint after frames 1-{full_frames} in full, untimed); CPU FP64 oracle on "
+                      f"{cores} threads"}
 
 
 def run_reference(args) -> None:
@@ -217,7 +223,7 @@ def run_reference(args) -> None:
     import scenes
 
     scene = scenes.body_scene(frames=args.warmup + args.steps + 1)
-    cpu = cpu_oracle_sample(scene, args.warmup, args.steps, args.cpu_substeps)
+    cpu = cpu_oracle_sample(scenes.body_scene(frames=args.warmup + 3), args.warmup + 1, args.steps, args.cpu_substeps)
     value = cpu["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -364,7 +370,7 @@ def run_ours(args) -> None:
     roofline = _roofline(main, fp64_peak.value)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        cpu = cpu_oracle_sample(scene, args.warmup, 1, args.cpu_substeps)
+        cpu = cpu_oracle_sample(scenes.body_scene(frames=args.warmup + 3), args.warmup + 1, 1, args.cpu_substeps)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
