@@ -634,11 +634,12 @@ KHS_API KhsResult khsxRollbackToFrame(KhsSolver *s, uint32_t frame)
     });
 }
 
-KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *s, uint32_t strands_per_warp, uint32_t blocks_per_sm)
+KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *s, uint32_t strands_per_warp, uint32_t blocks_per_sm,
+                                            uint32_t long_strands)
 {
     return guarded(s, [&] {
         if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
-        return s->engine->set_block_solve_schedule(strands_per_warp, blocks_per_sm);
+        return s->engine->set_block_solve_schedule(strands_per_warp, blocks_per_sm, long_strands);
     });
 }
 

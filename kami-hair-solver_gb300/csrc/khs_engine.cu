@@ -1444,7 +1444,7 @@ template<int H> struct AugLayout {
     static constexpr int kStrands = 32 / kLanes;     // strands per warp
 };
 
-template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, uint32_t g)
+template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, uint32_t g, uint32_t first = 0)
 {
     using L = AugLayout<H>;
     const unsigned FULL = 0xffffffffu;
@@ -1452,7 +1452,7 @@ template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, u
     const int grp = lane / L::kLanes, gl = lane % L::kLanes, r = gl % 6, h = gl / 6;
     const int base = grp * L::kLanes;
     const int c0 = h * L::kCols;  // first column of this lane
-    const uint32_t k = g * L::kStrands + uint32_t(grp);
+    const uint32_t k = first + g * L::kStrands + uint32_t(grp);
     const bool member = grp < L::kStrands && k < d.S;
     uint32_t begin = 0, len = 0;
     if (member) {
@@ -1608,6 +1608,25 @@ template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, u
         }
         if (on && h == 0) d.dir[6 * n + r] = value;
         next = on ? value : 0.0;
+    }
+}
+
+// Hybrid schedule: the `long_strands` longest strands one per warp with
+// 18 lanes each (the shortest chain per node), then the rest five per warp
+// with 6 lanes each (the fewest instructions per node overall).  Both
+// layouts compute every entry identically, so the split point does not
+// change the result.
+__global__ void __launch_bounds__(128) k_block_solve_hybrid(View d, uint32_t long_strands)
+{
+    const uint32_t rest = d.S > long_strands ? d.S - long_strands : 0;
+    const uint32_t groups = long_strands + (rest + AugLayout<1>::kStrands - 1) / AugLayout<1>::kStrands;
+    for (;;) {
+        uint32_t g = 0;
+        if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= groups) break;
+        if (g < long_strands) solve_group_aug<3>(d, g);
+        else solve_group_aug<1>(d, g - long_strands, long_strands);
     }
 }
 
@@ -2279,6 +2298,8 @@ struct Engine::Impl {
     double *ring = nullptr;
     std::vector<int64_t> ring_frame;
     void (*solve_kernel)(View) = nullptr;
+    uint32_t solve_long = 0;  // > 0: k_block_solve_hybrid with this many long strands
+    std::vector<uint32_t> sorted_len;  // free nodes per strand, in the solve order
     unsigned ff_blocks = 0;     // launch shape of the float-float kernels
     std::vector<KernelStat> kstats;
     std::vector<std::pair<size_t, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -2477,6 +2498,8 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     std::stable_sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) {
         return m.strand_count[l] - m.strand_fixed[l] > m.strand_count[r] - m.strand_fixed[r];
     });
+    I.sorted_len.resize(S);
+    for (size_t k = 0; k < S; ++k) I.sorted_len[k] = m.strand_count[order[k]] - m.strand_fixed[order[k]];
     std::vector<double> hcol(3 * Vn);
     for (size_t k = 0; k < Vn; ++k) { hcol[3 * k] = m.collider[k].x; hcol[3 * k + 1] = m.collider[k].y; hcol[3 * k + 2] = m.collider[k].z; }
     std::vector<double> hrx(3 * N), hrr(3 * N);
@@ -2750,16 +2773,22 @@ void Engine::make_steepest()
 // blocks of four warps per SM, chosen once by timing each on the first
 // system.  The choice does not change the result: both layouts compute every
 // entry with the same operations, and each strand is solved by one group.
-KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm)
+KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm, uint32_t long_strands)
 {
     Impl &I = *d_;
-    if (strands_per_warp == 0) { I.solve_blocks = 0; I.solve_kernel = nullptr; return KHS_OK; }
-    if ((strands_per_warp != 5 && strands_per_warp != 2 && strands_per_warp != 1) || blocks_per_sm < 1 || blocks_per_sm > 8)
+    if (strands_per_warp == 0) { I.solve_blocks = 0; I.solve_kernel = nullptr; I.solve_long = 0; return KHS_OK; }
+    if ((strands_per_warp != 5 && strands_per_warp != 2 && strands_per_warp != 1) || blocks_per_sm < 1 || blocks_per_sm > 8 ||
+        (long_strands && (strands_per_warp != 5 || long_strands >= I.v.S)))
         return KHS_ERROR_INVALID_ARGUMENT;
     int sms = 0;
     KHS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, kDevice));
-    const unsigned groups = unsigned((I.v.S + strands_per_warp - 1) / strands_per_warp);
-    I.solve_kernel = strands_per_warp == 5 ? k_block_solve_aug<1> : strands_per_warp == 2 ? k_block_solve_aug<2> : k_block_solve_aug<3>;
+    const unsigned groups = long_strands ? long_strands + unsigned((I.v.S - long_strands + 4) / 5)
+                                         : unsigned((I.v.S + strands_per_warp - 1) / strands_per_warp);
+    I.solve_kernel = long_strands ? nullptr
+                     : strands_per_warp == 5 ? k_block_solve_aug<1>
+                     : strands_per_warp == 2 ? k_block_solve_aug<2>
+                                             : k_block_solve_aug<3>;
+    I.solve_long = long_strands;
     I.solve_blocks = std::min(std::max(1u, (groups + 3) / 4), blocks_per_sm * unsigned(sms));
     const unsigned ff_groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
     I.ff_blocks = std::min(std::max(1u, (ff_groups + 3) / 4), 2u * unsigned(sms));
@@ -2774,12 +2803,13 @@ void Engine::tune_block_solve()
     cudaEvent_t ev[2];
     KHS_CUDA(cudaEventCreate(&ev[0]));
     KHS_CUDA(cudaEventCreate(&ev[1]));
-    auto time_it = [&](void (*kernel)(View), unsigned blocks) {
+    auto time_it = [&](void (*kernel)(View), unsigned blocks, uint32_t nlong) {
         float best = 3.0e38f;
         for (int rep = 0; rep < 2; ++rep) {
             KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
             KHS_CUDA(cudaEventRecord(ev[0], I.stream));
-            kernel<<<blocks, 128, 0, I.stream>>>(I.v);
+            if (kernel) kernel<<<blocks, 128, 0, I.stream>>>(I.v);
+            else k_block_solve_hybrid<<<blocks, 128, 0, I.stream>>>(I.v, nlong);
             ++I.launches;
             KHS_CUDA(cudaEventRecord(ev[1], I.stream));
             KHS_CUDA(cudaEventSynchronize(ev[1]));
@@ -2797,8 +2827,25 @@ void Engine::tune_block_solve()
         const unsigned most = std::max(1u, (groups + 3) / 4);
         for (unsigned per_sm = 1; per_sm <= 4; ++per_sm) {
             const unsigned blocks = std::min(most, per_sm * unsigned(sms));
-            const float ms = time_it(c.kernel, blocks);
-            if (ms < best_ms) { best_ms = ms; I.solve_kernel = c.kernel; I.solve_blocks = blocks; }
+            const float ms = time_it(c.kernel, blocks, 0);
+            if (ms < best_ms) { best_ms = ms; I.solve_kernel = c.kernel; I.solve_blocks = blocks; I.solve_long = 0; }
+            if (blocks == most) break;
+        }
+    }
+    // Hybrid: the strands of at least `cut` free nodes one per warp (18
+    // lanes), the rest five per warp.
+    uint32_t last_long = 0;
+    for (uint32_t cut : {160u, 128u, 96u, 64u, 48u}) {
+        const uint32_t nlong = uint32_t(std::count_if(I.sorted_len.begin(), I.sorted_len.end(),
+                                                       [&](uint32_t len) { return len >= cut; }));
+        if (nlong == 0 || nlong == last_long || nlong >= I.v.S) continue;
+        last_long = nlong;
+        const unsigned groups = nlong + unsigned((I.v.S - nlong + 4) / 5);
+        const unsigned most = std::max(1u, (groups + 3) / 4);
+        for (unsigned per_sm = 1; per_sm <= 3; ++per_sm) {
+            const unsigned blocks = std::min(most, per_sm * unsigned(sms));
+            const float ms = time_it(nullptr, blocks, nlong);
+            if (ms < best_ms) { best_ms = ms; I.solve_kernel = nullptr; I.solve_blocks = blocks; I.solve_long = nlong; }
             if (blocks == most) break;
         }
     }
@@ -2811,6 +2858,13 @@ void Engine::tune_block_solve()
     cudaEventDestroy(ev[1]);
     KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
     KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_failed, 0, sizeof(int), I.stream));
+}
+
+void Engine::launch_block_solve()
+{
+    Impl &I = *d_;
+    if (I.solve_kernel) I.launch("k_block_solve", I.solve_kernel, I.solve_blocks, 128, I.v);
+    else I.launch("k_block_solve", k_block_solve_hybrid, I.solve_blocks, 128, I.v, I.solve_long);
 }
 
 bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
@@ -2843,7 +2897,7 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
         }
     }
     if (fp64) {
-        I.launch("k_block_solve", I.solve_kernel, I.solve_blocks, 128, I.v);
+        launch_block_solve();
         I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
         I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
         I.check();

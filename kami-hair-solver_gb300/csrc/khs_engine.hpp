@@ -74,8 +74,9 @@ public:
 
     void set_mode(uint32_t mode) { mode_ = mode; }
     // Block-solve launch shape: 5, 2 or 1 strands per warp and blocks of four
-    // warps per SM; 0 strands per warp restores the one-time tuning.
-    KhsResult set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm);
+    // warps per SM (long_strands > 0 with 5: the longest strands one per
+    // warp first); 0 strands per warp restores the one-time tuning.
+    KhsResult set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm, uint32_t long_strands);
     uint32_t mode() const { return mode_; }
 
     KhsStepStats stats() const { return step_stats_; }
@@ -108,6 +109,7 @@ private:
     EvalStats evaluate(bool gradient, double dt, double alpha_for_trial);
     bool make_direction(KhsxSubstepRecord &rec, double grad_norm2);
     void tune_block_solve();
+    void launch_block_solve();
     void push_ring(uint32_t frame);
     void make_steepest();
     void limit_direction(double max_translation);

@@ -205,7 +205,7 @@ EXTENSION_FUNCTIONS = [
     ("khsxCopySubstepRecords", ctypes.c_int, [VP, P(SubstepRecord), c_u32]),
     ("khsxCopyContactRecords", ctypes.c_int, [VP, VP, c_u32]),
     ("khsxQueryContacts", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
-    ("khsxSetBlockSolveSchedule", ctypes.c_int, [VP, c_u32, c_u32]),
+    ("khsxSetBlockSolveSchedule", ctypes.c_int, [VP, c_u32, c_u32, c_u32]),
     ("khsxSetRollbackRing", ctypes.c_int, [VP, c_u32]),
     ("khsxRollbackToFrame", ctypes.c_int, [VP, c_u32]),
     ("khsxQueryContactsNoAlloc", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
@@ -488,8 +488,8 @@ class HairSolver:
     def rollback_to_frame(self, frame: int) -> None:
         self._check(self._library.khsxRollbackToFrame(self._handle, frame))
 
-    def set_block_solve_schedule(self, strands_per_warp: int, blocks_per_sm: int = 1) -> None:
-        self._check(self._library.khsxSetBlockSolveSchedule(self._handle, strands_per_warp, blocks_per_sm))
+    def set_block_solve_schedule(self, strands_per_warp: int, blocks_per_sm: int = 1, long_strands: int = 0) -> None:
+        self._check(self._library.khsxSetBlockSolveSchedule(self._handle, strands_per_warp, blocks_per_sm, long_strands))
 
     def query_contacts_no_alloc(self, q: np.ndarray, out: np.ndarray) -> int:
         """khsxQueryContactsNoAlloc into a caller-owned CONTACT_DTYPE array;
