@@ -92,10 +92,15 @@ KHS_HD void rotation_and_jacobian(V u, const double *ref, M &R, M *Jl)
         b = 0.5 - t2 / 24.0 + t2 * t2 / 720.0;
         s = 0.0; c = 1.0;
     } else {
-        const double t = sqrt(t2);
-        sincos(t, &s, &c);
-        a = s / t;
-        b = (1.0 - c) / t2;
+        // Half-angle form: one sincos, and 1 - cos t = 2 sin^2(t/2) without
+        // cancellation (it is also the left Jacobian's coefficient p).
+        const double t = sqrt(t2), it = 1.0 / t;
+        double sh, ch;
+        sincos(0.5 * t, &sh, &ch);
+        s = 2.0 * sh * ch;
+        c = 1.0 - 2.0 * sh * sh;
+        a = s * it;
+        b = 2.0 * sh * sh * (it * it);
     }
     // E = I + a W + b W^2 with W = [u]x.
     const double wx = u.x, wy = u.y, wz = u.z;
@@ -116,10 +121,9 @@ KHS_HD void rotation_and_jacobian(V u, const double *ref, M &R, M *Jl)
             p = 0.5 - t2 / 24.0 + t2 * t2 / 720.0 - t2 * t2 * t2 / 40320.0;
             r = 1.0 / 6.0 - t2 / 120.0 + t2 * t2 / 5040.0 - t2 * t2 * t2 / 362880.0;
         } else {
-            const double t = sqrt(t2);
-            const double sh = sin(0.5 * t);
-            p = 2.0 * sh * sh / t2;
-            r = (t - s) / (t2 * t);
+            const double t = sqrt(t2), it = 1.0 / t;
+            p = b;
+            r = (t - s) * (it * it * it);
         }
         M &J = *Jl;
         J.m[0] = 1.0 + r * w2[0]; J.m[1] = -p * wz + r * w2[1]; J.m[2] = p * wy + r * w2[2];

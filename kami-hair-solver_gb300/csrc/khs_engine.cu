@@ -1174,14 +1174,24 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_elem_eval(View 
                            &Jli, &Jlj);
         double a[6], b[6];
         dm::element_gradient(J, eps, d.w, L0, a, b);
+        // 16-byte stores: every block starts on a 16-byte boundary (36 and
+        // 6 doubles per node from 256-byte aligned arrays).
+        double2 *gi2 = reinterpret_cast<double2 *>(gi), *gj2 = reinterpret_cast<double2 *>(gj);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) { gi[k] = fi ? 0.0 : a[k]; gj[k] = fj ? 0.0 : b[k]; }
+        for (int k = 0; k < 3; ++k) {
+            gi2[k] = fi ? make_double2(0.0, 0.0) : make_double2(a[2 * k], a[2 * k + 1]);
+            gj2[k] = fj ? make_double2(0.0, 0.0) : make_double2(b[2 * k], b[2 * k + 1]);
+        }
         double hii[36], hjj[36], hij[36];
         dm::element_hessian(J, d.w, L0, hii, hjj, hij);
-        for (int k = 0; k < 36; ++k) {
-            Hii[k] = fi ? 0.0 : hii[k];
-            Hjj[k] = fj ? 0.0 : hjj[k];
-            Hij[k] = (fi || fj) ? 0.0 : hij[k];
+        double2 *Hii2 = reinterpret_cast<double2 *>(Hii), *Hjj2 = reinterpret_cast<double2 *>(Hjj);
+        double2 *Hij2 = reinterpret_cast<double2 *>(Hij);
+        const bool fij = fi || fj;
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+            Hii2[k] = fi ? make_double2(0.0, 0.0) : make_double2(hii[2 * k], hii[2 * k + 1]);
+            Hjj2[k] = fj ? make_double2(0.0, 0.0) : make_double2(hjj[2 * k], hjj[2 * k + 1]);
+            Hij2[k] = fij ? make_double2(0.0, 0.0) : make_double2(hij[2 * k], hij[2 * k + 1]);
         }
     } else {
         dm::element_strain(Ri, Rj, xi, xj, L0, load3(d.gamma0 + 3 * size_t(e)), load3(d.kappa0 + 3 * size_t(e)), eps,
