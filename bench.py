@@ -65,9 +65,9 @@ MEASURED_PEAKS = REPO / "MEASURED_PEAKS.json"
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # dominant kernels from one ncu capture of this workload; see profiles/.
-# k_contact was captured early in frame 5 (its traffic follows the contact
-# state); k_block_solve's does not depend on the state.
-NCU_TRAFFIC_BYTES: dict[str, float] = {"k_contact": 29.547776e6 + 5.12e3, "k_block_solve": 190.322688e6 + 67.055616e6}
+# (k_block_solve's traffic does not depend on the contact state.)
+NCU_TRAFFIC_BYTES: dict[str, float] = {"k_block_solve": 181.063424e6 + 64.278016e6,
+                                      "k_elem_eval_grad": 89.102592e6 + 211.5456e6}
 
 
 def algorithmic(name: str, nodes: int, free_nodes: int, elements: int, candidates: float):
