@@ -17,13 +17,22 @@
 //                  indices (stackless traversal) and parent links (one-launch
 //                  bottom-up refit)
 //
-// Kernels (one thread per node / element / strand / BVH leaf):
-//   k_begin_substep, k_collider_interp, k_refit, k_sweep(+record),
-//   k_precond, k_node_eval, k_elem_eval, k_node_sum, k_reduce_eval,
-//   k_final_eval, k_block_solve_aug, k_steepest, k_scale, k_reduce_dir,
-//   k_final_dir, k_ccd, k_update_velocity, k_friction, k_friction_apply,
-//   k_gather.  Reductions are two-level (fixed per-block trees, then one
-//   block over the partials) and therefore deterministic.
+// Kernels (thread per node / element / BVH leaf unless noted):
+//   per substep   k_begin_substep, k_collider_interp, k_tri32, k_refit,
+//                 k_sweep(+record), k_precond, k_update_velocity,
+//                 k_friction(+apply)
+//   evaluation    k_node_eval, [mixed: k_contact_filter, k_contact_near (warp
+//                 per element with cached leaves), k_contact_exact (thread per
+//                 FP32 survivor), k_contact_select], k_elem_eval, k_node_sum
+//                 (thread per block entry), k_reduce_eval, k_final_eval
+//   direction     k_block_solve_aug<H> / k_block_solve_hybrid (persistent
+//                 warps, strand groups from a longest-first queue),
+//                 [float-float form: k_ff_factor, k_ff_residual, k_ff_correct],
+//                 k_steepest, k_scale, k_reduce_dir, k_final_dir
+//   CCD           k_ccd (plain), k_ccd_collect + k_ccd_pairs (mixed)
+//   queries       k_contact, k_contact_query_records, k_gather
+// Reductions are two-level (fixed per-block trees, then one block over the
+// partials) and therefore deterministic.
 #include "khs_engine.hpp"
 #include "khs_device_math.cuh"
 #include "khs_ff.cuh"
@@ -140,8 +149,7 @@ struct View {
     // and the element's node positions when they were collected.
     uint32_t *cache_leaf;
     uint8_t *cache_n;
-    double *cache_x;
-    float *cache_x32;  // FP32 copy of cache_x for the filter's slack test
+    float *cache_x32;  // FP32 node positions when the leaves were collected [E][6]
     // Mixed contact pass in three launches: FP32 vertex records of every
     // triangle in leaf order (a, b, c as three float4, the triangle index in
     // the first .w), the survivors of the FP32 filter per element (at most
@@ -715,7 +723,7 @@ __device__ __forceinline__ uint32_t closest_triangle(const View &d, V xi, V xj, 
 // closest triangle with its closest pair, gap and flags.  The mixed form runs
 // this as its own low-register pass before the element energy (and for the
 // contact-query entry point); the plain form searches inside k_elem_eval.
-template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact(View d, const double *q, int cache)
+template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact(View d, const double *q)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
@@ -727,33 +735,7 @@ template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_contact(View d,
     pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
     if (d.has_collider && !d.fixed[i] && d.econtact[e]) {
         const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
-        const double pad = d.radius + d.offset + d.dhat;
-        if (MIXED && cache >= 0) {
-            uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
-            double *cx = d.cache_x + 6 * size_t(e);
-            if (cache == 1) {
-                // First evaluation after a refit: collect the leaves around
-                // the element box grown by the slack.
-                const V s3 = dm::v(kCacheSlack, kCacheSlack, kCacheSlack);
-                const uint32_t n = collect_leaves(d, dm::vmin(xi, xj) - s3, dm::vmax(xi, xj) + s3, pad, slots, kCacheLeaves);
-                d.cache_n[e] = n <= uint32_t(kCacheLeaves) ? uint8_t(n) : kCacheInvalid;
-                store3(cx, xi);
-                store3(cx + 3, xj);
-            }
-            const uint8_t n = d.cache_n[e];
-            const V ci = load3(cx), cj = load3(cx + 3);
-            const bool inside = n != kCacheInvalid && fabs(xi.x - ci.x) <= kCacheSlack && fabs(xi.y - ci.y) <= kCacheSlack &&
-                                fabs(xi.z - ci.z) <= kCacheSlack && fabs(xj.x - cj.x) <= kCacheSlack &&
-                                fabs(xj.y - cj.y) <= kCacheSlack && fabs(xj.z - cj.z) <= kCacheSlack;
-            if (inside) {
-                const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
-                closest = closest_triangle_in(d, xi, xj, cand, pair, [&](auto &&fn) { leaves_query(d, slots, n, lo, hi, pad, fn); });
-            } else {
-                closest = closest_triangle<MIXED>(d, xi, xj, pad, cand, pair);
-            }
-        } else {
-            closest = closest_triangle<MIXED>(d, xi, xj, pad, cand, pair);
-        }
+        closest = closest_triangle<MIXED>(d, xi, xj, d.radius + d.offset + d.dhat, cand, pair);
         if (closest != kNone) {
             flags |= kFlagClosest;
             gap = pair.distance - d.radius - d.offset;
@@ -2415,7 +2397,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     bytes += 2 * padded<float>(3 * B) + padded<float4>(2 * B);
     const size_t pair_capacity = std::min<size_t>(std::max<size_t>(size_t(1) << 20, 8 * E), size_t(16) << 20);
     bytes += 2 * padded<double>(E) + padded<double>(3 * E) + 2 * padded<uint32_t>(pair_capacity);
-    bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E) + padded<double>(6 * E);
+    bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E);
     bytes += padded<float>(3 * N) + padded<float>(6 * E);
     bytes += padded<uint32_t>(E);
     bytes += 2 * padded<float2>(36 * N) + padded<float2>(6 * N) + padded<float>(N);
@@ -2466,7 +2448,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.c_t = a.take<double>(E); v.c_dist = a.take<double>(E); v.c_bary = a.take<double>(3 * E);
     v.pair_elem = a.take<uint32_t>(pair_capacity); v.pair_tri = a.take<uint32_t>(pair_capacity);
     v.pair_capacity = uint32_t(pair_capacity);
-    v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E); v.cache_x = a.take<double>(6 * E);
+    v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E);
     v.cache_x32 = a.take<float>(6 * E);
     v.tri32 = a.take<float4>(3 * T);
     v.ff_inv = a.take<float2>(36 * N); v.ff_c = a.take<float2>(36 * N); v.ff_d = a.take<float2>(6 * N);
@@ -3354,7 +3336,7 @@ KhsResult Engine::query_contacts(const double *q, uint64_t dof, KhsxContactRecor
     if (!q || dof < 6 * uint64_t(I.v.N) || !out || capacity < I.v.E) return KHS_ERROR_INVALID_ARGUMENT;
     KHS_CUDA(cudaMemcpyAsync(I.v.q_base, q, 6 * size_t(I.v.N) * 8, cudaMemcpyHostToDevice, I.stream));
     I.launch("k_contact_query", mode_ ? k_contact<true> : k_contact<false>, grid_for(I.v.E), kBlock, I.v,
-             static_cast<const double *>(I.v.q_base), -1);
+             static_cast<const double *>(I.v.q_base));
     KHS_CUDA(cudaGetLastError());
     return copy_contact_records(out, capacity);
 }
