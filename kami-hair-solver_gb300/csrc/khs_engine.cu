@@ -93,7 +93,7 @@ struct Scalars {
     uint32_t solve_next;  // next strand group of the block-solve work queue
     uint32_t refine_bits; // largest relative refinement correction (FP32 bits)
     uint32_t near_count;  // elements queued for the warp-cooperative contact pass
-    uint32_t pad;
+    uint32_t ccd_near;    // elements queued for the warp-cooperative CCD pass
 };
 
 struct Partial {
@@ -2010,6 +2010,7 @@ __global__ void __launch_bounds__(kBlock) k_final_dir(View d)
         d.sc->solve_failed = 0;
         d.sc->pair_count = 0;
         d.sc->solve_next = 0;
+        d.sc->ccd_near = 0;
         d.sc->refine_bits = 0;
     }
 }
@@ -2115,8 +2116,53 @@ __global__ void __launch_bounds__(kBlock) k_ccd_collect(View d)
         const dm::F3 a0 = dm::f3(float(e0.x), float(e0.y), float(e0.z)), a1 = dm::f3(float(e1.x), float(e1.y), float(e1.z));
         cached = within_cache_slack(c, origin, xj32) && within_cache_slack(c, a0, a1);
     }
-    if (cached) leaves_positions(d, d.cache_leaf + size_t(kCacheLeaves) * e, nl, qb, test);
-    else bvh_positions_packed(d, qb, test);
+    if (cached) {
+        // k_ccd_near tests the cached leaves, one warp per element.
+        if (nl > 0) d.near_list[atomicAdd(&d.sc->ccd_near, 1u)] = e;
+    } else {
+        bvh_positions_packed(d, qb, test);
+    }
+}
+
+// One warp per element queued by k_ccd_collect: lane l tests cached leaf l
+// against the swept box and applies the same FP32 skip bound to that leaf's
+// triangles (the pair order does not matter: the bound is a minimum).
+__global__ void __launch_bounds__(kBlock) k_ccd_near(View d)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t count = d.sc->ccd_near;
+    const double target = d.radius + d.offset + d.min_gap;
+    const float target_ru = __double2float_ru(target);
+    for (uint32_t k = warp; k < count; k += nwarps) {
+        const uint32_t e = d.near_list[k];
+        const uint32_t nl = d.cache_n[e];
+        if (uint32_t(lane) >= nl) continue;
+        const uint32_t i = d.ei[e], j = d.ej[e];
+        const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
+        const V d0 = load3(d.dir + 6 * size_t(i)), d1 = load3(d.dir + 6 * size_t(j));
+        const double speed = fmax(dm::gnorm(d0), dm::gnorm(d1));
+        const V e0 = p0 + d0, e1 = p1 + d1;
+        const QueryBox qb = make_query(dm::vmin(dm::vmin(p0, p1), dm::vmin(e0, e1)), dm::vmax(dm::vmax(p0, p1), dm::vmax(e0, e1)),
+                                       target);
+        const dm::F3 origin = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
+        const dm::F3 f0 = dm::f3(0.f, 0.f, 0.f);
+        const dm::F3 f1 = dm::f3(d.q32[3 * size_t(j)] - origin.x, d.q32[3 * size_t(j) + 1] - origin.y,
+                                 d.q32[3 * size_t(j) + 2] - origin.z);
+        const float speed_ru = __fmul_ru(__double2float_ru(speed), 1.000002f);
+        const uint32_t node = d.cache_leaf[size_t(kCacheLeaves) * e + lane];
+        const float4 a = __ldg(d.bnode + 2 * size_t(node)), b = __ldg(d.bnode + 2 * size_t(node) + 1);
+        if (!maybe_overlap(qb, a, b) || !leaf_overlap_exact(d, node, a, b, qb)) continue;
+        const uint32_t leaf = __float_as_uint(b.w), first = leaf >> 4, cnt = leaf & 15u;
+        for (uint32_t p = first; p < first + cnt; ++p) {
+            float m;
+            uint32_t t;
+            const float df = record_distance_f(d, p, origin, f0, f1, m, t);
+            if (__fmul_rd(0.8f, __fsub_rd(__fsub_rd(df, m), target_ru)) >= speed_ru) continue;
+            const uint32_t slot = atomicAdd(&d.sc->pair_count, 1u);
+            if (slot < d.pair_capacity) { d.pair_elem[slot] = e; d.pair_tri[slot] = t; }
+        }
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_ccd_pairs(View d)
@@ -2229,6 +2275,7 @@ __global__ void k_init_scalars(View d)
     d.sc->solve_next = 0;
     d.sc->refine_bits = 0;
     d.sc->near_count = 0;
+    d.sc->ccd_near = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -2953,6 +3000,7 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
                 progress_phase_.store(KHS_PHASE_CCD);
                 if (mode_) {
                     I.launch("k_ccd_collect", k_ccd_collect, grid_for(v.E), kBlock, v);
+                    I.launch("k_ccd_near", k_ccd_near, 152u * 8u, kBlock, v);
                     I.launch("k_ccd_pairs", k_ccd_pairs, 152u * 8u, kBlock, v);
                 } else {
                     I.launch("k_ccd", k_ccd<false>, grid_for(v.E), kBlock, v);
