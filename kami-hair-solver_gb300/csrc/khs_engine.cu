@@ -155,7 +155,7 @@ struct View {
     // the first .w), the survivors of the FP32 filter per element (at most
     // kSurvivors, in traversal order), their FP64 closest pairs (distance,
     // t, barycentrics) and the (element, slot) work list of the FP64 pass.
-    float4 *tri32;
+    float4 *tri32, *tri32_old;  // FP32 records of col_cur and col_old
     // Mixed-form factors in float-float (hi, lo): B_n^-1 and C_n rows [N][36],
     // d'_n [N][6], and the diagonal shift used at each node.
     float2 *ff_inv, *ff_c, *ff_d;
@@ -507,6 +507,38 @@ __global__ void __launch_bounds__(kBlock) k_refit(View d, int swept)
 // Mixed form: a candidate whose FP32 lower-bound clearance already lets the
 // first advancement step reach alpha = 1 cannot fail and is skipped (the
 // 1e-6 relative slack dwarfs the FP64 rounding of that one step).
+// FP32 pre-test of the mixed sweep for the candidate at leaf-order position
+// p: true when the first conservative-advancement step of the exact pass is
+// certain to reach the end of the substep (no failure from this triangle).
+// It needs a lower bound of the segment's distance to the triangle at its
+// old position (tri32_old records, margins as record_distance_f) and an
+// upper bound of the largest vertex displacement (FP32 differences of the
+// rounded copies, widened by their rounding).
+__device__ __forceinline__ bool sweep_skip_f(const View &d, uint32_t p, dm::F3 origin, dm::F3 f1, float target_ru)
+{
+    const float4 n0 = __ldg(d.tri32 + 3 * size_t(p)), n1 = __ldg(d.tri32 + 3 * size_t(p) + 1),
+                 n2 = __ldg(d.tri32 + 3 * size_t(p) + 2);
+    const float4 o0 = __ldg(d.tri32_old + 3 * size_t(p)), o1 = __ldg(d.tri32_old + 3 * size_t(p) + 1),
+                 o2 = __ldg(d.tri32_old + 3 * size_t(p) + 2);
+    auto disp = [](float4 a, float4 b) {
+        const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        const float mag = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)), fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fabsf(b.z)));
+        return __fadd_ru(__fmul_ru(sqrtf(dx * dx + dy * dy + dz * dz), 1.00001f), __fmaf_ru(mag, 5.0e-7f, 1.0e-12f));
+    };
+    const float speed_ub = fmaxf(disp(n0, o0), fmaxf(disp(n1, o1), disp(n2, o2)));
+    const dm::F3 a = dm::f3(o0.x - origin.x, o0.y - origin.y, o0.z - origin.z);
+    const dm::F3 b = dm::f3(o1.x - origin.x, o1.y - origin.y, o1.z - origin.z);
+    const dm::F3 c = dm::f3(o2.x - origin.x, o2.y - origin.y, o2.z - origin.z);
+    float m;
+    const float df = dm::segment_triangle_distance_f(dm::f3(0.f, 0.f, 0.f), f1, a, b, c, m);
+    const float vmax = fmaxf(fmaxf(fmaxf(fabsf(o0.x), fabsf(o0.y)), fmaxf(fabsf(o0.z), fabsf(o1.x))),
+                             fmaxf(fmaxf(fabsf(o1.y), fabsf(o1.z)), fmaxf(fmaxf(fabsf(o2.x), fabsf(o2.y)), fabsf(o2.z))));
+    const float omax = fmaxf(fmaxf(fabsf(origin.x), fabsf(origin.y)), fabsf(origin.z));
+    const float emax = fmaxf(fmaxf(fabsf(f1.x), fabsf(f1.y)), fabsf(f1.z)) + omax;
+    m += 2.5e-7f * (vmax + omax + emax) + 1.0e-9f;
+    return __fmul_rd(0.8f, __fsub_rd(__fsub_rd(df, m), target_ru)) >= __fmul_ru(speed_ub, 1.000002f);
+}
+
 template<bool MIXED> __device__ bool sweep_element(const View &d, uint32_t e, SweepRecord *rec)
 {
     const uint32_t i = d.ei[e], j = d.ej[e];
@@ -554,12 +586,50 @@ template<bool MIXED> __device__ bool sweep_element(const View &d, uint32_t e, Sw
     return failed;
 }
 
+// Mixed sweep of one element: the same candidates in the same order as
+// sweep_element, with sweep_skip_f deciding first from FP32 copies, so only
+// the triangles that could fail are loaded and advanced in FP64.
+__device__ bool sweep_element_f(const View &d, uint32_t e)
+{
+    const uint32_t i = d.ei[e], j = d.ej[e];
+    const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
+    const double target = d.radius + d.offset + d.min_gap;
+    const float target_ru = __double2float_ru(target);
+    const dm::F3 origin = dm::f3(float(p0.x), float(p0.y), float(p0.z));
+    const dm::F3 f1 = dm::f3(float(p1.x) - origin.x, float(p1.y) - origin.y, float(p1.z) - origin.z);
+    bool failed = false;
+    bvh_positions_packed(d, make_query(dm::vmin(p0, p1), dm::vmax(p0, p1), target), [&](uint32_t p) {
+        if (failed || sweep_skip_f(d, p, origin, f1, target_ru)) return;
+        const uint32_t t = __float_as_uint(__ldg(d.tri32 + 3 * size_t(p)).w);
+        const V oa = load3(d.col_old + 3 * size_t(d.tri[3 * t])), ob = load3(d.col_old + 3 * size_t(d.tri[3 * t + 1])),
+                oc = load3(d.col_old + 3 * size_t(d.tri[3 * t + 2]));
+        const V da = dm::gsub(tri_vertex(d, t, 0), oa), db = dm::gsub(tri_vertex(d, t, 1), ob),
+                dc = dm::gsub(tri_vertex(d, t, 2), oc);
+        const double speed = fmax(dm::gnorm(da), fmax(dm::gnorm(db), dm::gnorm(dc)));
+        if (speed < 1e-30) return;
+        double alpha = 0.0;
+        bool end = false;
+        for (int k = 0; k < 80; ++k) {
+            const V a = dm::gadd(oa, dm::gmul(da, alpha)), b = dm::gadd(ob, dm::gmul(db, alpha)), c = dm::gadd(oc, dm::gmul(dc, alpha));
+            const double clearance = dm::closest_segment_triangle(p0, p1, a, b, c).distance - target;
+            if (clearance <= 0) { failed = true; break; }
+            const double advance = 0.8 * clearance / speed;
+            if (alpha + advance >= 1) { end = true; break; }
+            if (advance < 1e-12) { failed = true; break; }
+            alpha += advance;
+        }
+        if (!end) failed = true;
+    });
+    return failed;
+}
+
 template<bool MIXED> __global__ void __launch_bounds__(kBlock) k_sweep(View d)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
     if (d.fixed[d.ei[e]] || !d.econtact[e]) return;
-    if (sweep_element<MIXED>(d, e, nullptr)) atomicMin(&d.sc->sweep_fail, e);
+    const bool failed = MIXED ? sweep_element_f(d, e) : sweep_element<false>(d, e, nullptr);
+    if (failed) atomicMin(&d.sc->sweep_fail, e);
 }
 
 // Publishes the lowest failing element of k_sweep (with its first failing
@@ -768,8 +838,8 @@ constexpr int kSurvivors = 8;
 constexpr int kLeafTriangles = 8;  // BVH leaves hold at most 8 triangles (cuda_backend.cu:305)
 constexpr uint8_t kSurvOverflow = 0xff;
 
-// FP32 vertex records of every triangle in leaf order; run whenever col_cur
-// changes (after k_collider_interp and at set-up).
+// FP32 vertex records of every triangle in leaf order, of col_cur and of
+// col_old; run whenever they change (after k_collider_interp and at set-up).
 __global__ void __launch_bounds__(kBlock) k_tri32(View d)
 {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -779,6 +849,11 @@ __global__ void __launch_bounds__(kBlock) k_tri32(View d)
     d.tri32[3 * size_t(p)] = make_float4(float(a.x), float(a.y), float(a.z), __uint_as_float(t));
     d.tri32[3 * size_t(p) + 1] = make_float4(float(b.x), float(b.y), float(b.z), 0.0f);
     d.tri32[3 * size_t(p) + 2] = make_float4(float(c.x), float(c.y), float(c.z), 0.0f);
+    const V oa = load3(d.col_old + 3 * size_t(d.tri[3 * t])), ob = load3(d.col_old + 3 * size_t(d.tri[3 * t + 1])),
+            oc = load3(d.col_old + 3 * size_t(d.tri[3 * t + 2]));
+    d.tri32_old[3 * size_t(p)] = make_float4(float(oa.x), float(oa.y), float(oa.z), __uint_as_float(t));
+    d.tri32_old[3 * size_t(p) + 1] = make_float4(float(ob.x), float(ob.y), float(ob.z), 0.0f);
+    d.tri32_old[3 * size_t(p) + 2] = make_float4(float(oc.x), float(oc.y), float(oc.z), 0.0f);
 }
 
 // candidate_distance_f on the record at leaf-order position p (one 48-byte
@@ -2448,7 +2523,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     bytes += padded<float>(3 * N) + padded<float>(6 * E);
     bytes += padded<uint32_t>(E);
     bytes += 2 * padded<float2>(36 * N) + padded<float2>(6 * N) + padded<float>(N);
-    bytes += padded<float4>(3 * T) + 2 * padded<uint32_t>(size_t(kSurvivors) * E) + padded<uint8_t>(E) +
+    bytes += 2 * padded<float4>(3 * T) + 2 * padded<uint32_t>(size_t(kSurvivors) * E) + padded<uint8_t>(E) +
              padded<double>(5 * size_t(kSurvivors) * E);
     bytes += 2 * padded<double>(3 * B) + 4 * padded<uint32_t>(B) + padded<int32_t>(B) + 2 * padded<uint32_t>(B) +
              padded<uint32_t>(L) + padded<uint32_t>(T);
@@ -2497,7 +2572,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.pair_capacity = uint32_t(pair_capacity);
     v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E);
     v.cache_x32 = a.take<float>(6 * E);
-    v.tri32 = a.take<float4>(3 * T);
+    v.tri32 = a.take<float4>(3 * T); v.tri32_old = a.take<float4>(3 * T);
     v.ff_inv = a.take<float2>(36 * N); v.ff_c = a.take<float2>(36 * N); v.ff_d = a.take<float2>(6 * N);
     v.ff_shift = a.take<float>(N);
     v.surv_tri = a.take<uint32_t>(size_t(kSurvivors) * E); v.surv_list = a.take<uint32_t>(size_t(kSurvivors) * E);
