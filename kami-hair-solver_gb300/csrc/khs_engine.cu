@@ -950,12 +950,13 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
         if (enabled) {
             const dm::F3 xi32 = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
             const dm::F3 xj32 = dm::f3(d.q32[3 * size_t(j)], d.q32[3 * size_t(j) + 1], d.q32[3 * size_t(j) + 2]);
-            const V xi = load3(q + 6 * size_t(i)), xj = load3(q + 6 * size_t(j));
             const double pad = d.radius + d.offset + d.dhat;
-            const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
             float *c32 = d.cache_x32 + 6 * size_t(e);
             uint8_t nl = cache >= 0 ? d.cache_n[e] : kCacheInvalid;
             bool inside = cache == 0 && nl != kCacheInvalid && within_cache_slack(c32, xi32, xj32);
+            // FP64 positions only where a walk is needed.
+            V xi = dm::v(0, 0, 0), xj = xi;
+            if (!inside) { xi = load3(q + 6 * size_t(i)); xj = load3(q + 6 * size_t(j)); }
             if (cache == 1 || (cache == 0 && !inside)) {
                 // (Re)collect the leaves around the element box grown by the
                 // slack: one walk, after which both filter passes read the
@@ -969,9 +970,6 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
                 c32[0] = xi32.x; c32[1] = xi32.y; c32[2] = xi32.z; c32[3] = xj32.x; c32[4] = xj32.y; c32[5] = xj32.z;
                 inside = nl != kCacheInvalid;
             }
-            const float lo32[3] = {fminf(xi32.x, xj32.x), fminf(xi32.y, xj32.y), fminf(xi32.z, xj32.z)};
-            const float hi32[3] = {fmaxf(xi32.x, xj32.x), fmaxf(xi32.y, xj32.y), fmaxf(xi32.z, xj32.z)};
-            const QueryBox qb = make_query_f(lo32, hi32, dm::vmin(xi, xj), dm::vmax(xi, xj), pad);
             if (inside) {
                 if (nl > 0) {
                     // k_contact_near finishes the element, one warp over its leaves.
@@ -979,6 +977,10 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
                     deferred = true;
                 }
             } else {
+                // More than kCacheLeaves leaves around the element: walk.
+                const float lo32[3] = {fminf(xi32.x, xj32.x), fminf(xi32.y, xj32.y), fminf(xi32.z, xj32.z)};
+                const float hi32[3] = {fmaxf(xi32.x, xj32.x), fmaxf(xi32.y, xj32.y), fmaxf(xi32.z, xj32.z)};
+                const QueryBox qb = make_query_f(lo32, hi32, dm::vmin(xi, xj), dm::vmax(xi, xj), pad);
                 n = filter_survivors(d, e, xi32, xj32, cand, [&](auto &&fn) { bvh_positions_packed(d, qb, fn); });
             }
         }
