@@ -2843,7 +2843,8 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
              trial ? 1 : 0, trial ? alpha : 0.0, dt);
     if (mode_ && v.has_collider) {
         const double *q = v.q;
-        I.launch(rebuild_cache_ ? "k_contact_filter_rebuild" : "k_contact_filter", k_contact_filter, grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
+        I.launch(rebuild_cache_ ? "k_contact_filter_rebuild" : trial ? "k_contact_filter_trial" : "k_contact_filter", k_contact_filter,
+                 grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
         I.launch("k_contact_near", k_contact_near, 152 * 8, kBlock, v);
         I.launch("k_contact_exact", k_contact_exact, 152 * 4, kBlock, v, q);
         I.launch("k_contact_select", k_contact_select, grid_for(v.E), kBlock, v, q);
