@@ -513,6 +513,20 @@ KHS_API KhsResult khsxQueryContactsNoAlloc(KhsSolver *solver, const double *q,
                                            KhsxContactRecord *records,
                                            uint32_t capacity);
 
+/* Root targets of every internal node for evaluated source points: the
+   positions and rotation vectors khsUpdateRootTargets and
+   khsSetRootAnimationFrame hand to the solver (replaces the host pass
+   Solver::compute_root_targets, src/solver.cpp:416-447, which those entry
+   points run per call in the reference).  All three entry points compute
+   them on the device.  point_count must equal the curves' point count and
+   node_capacity at least the internal node count; positions and rotations
+   receive node_capacity >= N entries.  Errors: KHS_ERROR_INVALID_ARGUMENT
+   (unbuilt solver, count or capacity), KHS_ERROR_INVALID_HAIR (a non-finite
+   coordinate or a degenerate tangent). */
+KHS_API KhsResult khsxComputeRootTargets(KhsSolver *solver, const KhsVec3 *points,
+                                         uint32_t point_count, KhsVec3 *positions,
+                                         KhsVec3 *rotations, uint32_t node_capacity);
+
 /* ---- measurement ------------------------------------------------------- */
 
 /* With profiling on, every kernel launch of the solver is bracketed by CUDA

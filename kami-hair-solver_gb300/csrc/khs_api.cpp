@@ -267,35 +267,35 @@ struct KhsSolver {
         return KHS_OK;
     }
 
-    KhsResult convert_roots(const KhsVec3 *p, uint32_t n, std::vector<Vec> &pos, std::vector<Vec> &rot, KhsResult bad_point,
-                            KhsResult bad_count)
+    // Source points of new root targets: the solver must be built, the
+    // count must match the curves, every coordinate finite
+    // (solver.cpp:802-811).  The targets themselves are computed on the
+    // device by the engine.
+    KhsResult check_root_points(const KhsVec3 *p, uint32_t n, KhsResult bad_point, KhsResult bad_count)
     {
-        if (!built || !p || n != input.points.size()) {
+        if (!built || !engine || !p || n != input.points.size()) {
             error = "the root target point count does not match the source curves";
             return bad_count;
         }
-        std::vector<Vec> pts(n);
-        for (uint32_t i = 0; i < n; ++i) {
+        for (uint32_t i = 0; i < n; ++i)
             if (!finite3(p[i])) {
                 error = "root targets have a non-finite coordinate";
                 return bad_point;
             }
-            pts[i] = to_vec(p[i]);
-        }
-        if (!khs::root_targets(model, pts, pos, rot)) {
-            error = "cannot compute root directions from the root targets";
-            return KHS_ERROR_INVALID_HAIR;
-        }
         return KHS_OK;
     }
 
     KhsResult update_roots(const KhsVec3 *p, uint32_t n)
     {
-        std::vector<Vec> pos, rot;
-        const KhsResult r = convert_roots(p, n, pos, rot, KHS_ERROR_INVALID_HAIR, KHS_ERROR_INVALID_ARGUMENT);
+        const KhsResult r = check_root_points(p, n, KHS_ERROR_INVALID_HAIR, KHS_ERROR_INVALID_ARGUMENT);
         if (r != KHS_OK) return r;
-        engine->set_pending_roots(pos, rot);
-        return KHS_OK;
+        return from_engine(engine->set_pending_root_points(p, n));
+    }
+
+    KhsResult from_engine(KhsResult r)
+    {
+        if (r != KHS_OK) error = engine->last_error();
+        return r;
     }
 
     KhsResult after_engine(KhsResult r)
@@ -459,13 +459,9 @@ KHS_API KhsResult khsAllocateAnimation(KhsSolver *s, uint32_t frame_count)
 KHS_API KhsResult khsSetRootAnimationFrame(KhsSolver *s, uint32_t frame_index, const KhsVec3 *points, uint32_t point_count)
 {
     return guarded(s, [&] {
-        if (!s->built || !s->engine || !points || point_count != s->input.points.size()) return KHS_ERROR_INVALID_ARGUMENT;
-        std::vector<Vec> pos, rot;
-        const KhsResult c = s->convert_roots(points, point_count, pos, rot, KHS_ERROR_INVALID_HAIR, KHS_ERROR_INVALID_ARGUMENT);
+        const KhsResult c = s->check_root_points(points, point_count, KHS_ERROR_INVALID_HAIR, KHS_ERROR_INVALID_ARGUMENT);
         if (c != KHS_OK) return c;
-        const KhsResult r = s->engine->set_root_animation_frame(frame_index, pos, rot);
-        if (r != KHS_OK) s->error = s->engine->last_error();
-        return r;
+        return s->from_engine(s->engine->set_root_animation_frame(frame_index, points, point_count));
     });
 }
 
@@ -684,6 +680,20 @@ KHS_API KhsResult khsxQueryContactsNoAlloc(KhsSolver *s, const double *q, uint64
     if (!s) return KHS_ERROR_INVALID_ARGUMENT;
     if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
     return s->engine->query_contacts_no_alloc(q, dof_count, records, capacity);
+}
+
+KHS_API KhsResult khsxComputeRootTargets(KhsSolver *s, const KhsVec3 *points, uint32_t point_count, KhsVec3 *positions,
+                                         KhsVec3 *rotations, uint32_t node_capacity)
+{
+    return guarded(s, [&] {
+        const KhsResult c = s->check_root_points(points, point_count, KHS_ERROR_INVALID_HAIR, KHS_ERROR_INVALID_ARGUMENT);
+        if (c != KHS_OK) return c;
+        if (!positions || !rotations || node_capacity < s->model.nodes()) {
+            s->error = "the root target output arrays are smaller than the internal node count";
+            return KHS_ERROR_INVALID_ARGUMENT;
+        }
+        return s->from_engine(s->engine->root_targets_to_host(points, point_count, positions, rotations));
+    });
 }
 
 KHS_API KhsResult khsxSetProfiling(KhsSolver *s, uint32_t enable)

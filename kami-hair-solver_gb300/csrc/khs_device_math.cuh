@@ -542,5 +542,162 @@ KHS_HD double barrier_energy_gradient(V x0, V x1, double t, V body_point, double
     return energy;
 }
 
+// ---- root targets (src/solver.cpp:416-447, src/math.hpp:26-58) -----------
+//
+// Frames of the driven nodes: a frame per node whose third column is the
+// unit tangent, the first column carried from node to node by the minimal
+// rotation between consecutive tangents, and the rotation vector of
+// frame * reference^T (src/solver.cpp:19-26 goes through Eigen's AngleAxis;
+// restated with Shepperd's method, J. Guidance and Control 1(3), 1978).
+// Written with the non-contracting operations above and correctly rounded
+// division and square root, so the device rounds like host code built with
+// -ffp-contract=off: positions, tangents and frames agree bit for bit and the
+// rotation vectors differ only through atan2.
+
+#if defined(__CUDA_ARCH__)
+KHS_HD bool gfinite(double x) { return isfinite(x); }
+#else
+KHS_HD bool gfinite(double x) { return std::isfinite(x); }
+#endif
+
+KHS_HD V gcross(V a, V b)
+{
+    return v(xs(xm(a.y, b.z), xm(a.z, b.y)), xs(xm(a.z, b.x), xm(a.x, b.z)), xs(xm(a.x, b.y), xm(a.y, b.x)));
+}
+
+// Unit vector with Eigen's normalized() semantics: a zero (or NaN) squared
+// norm leaves the vector unchanged; each component is divided.
+KHS_HD V gunit(V a)
+{
+    const double n2 = gdot(a, a);
+    if (!(n2 > 0.0)) return a;
+    const double n = sqrt(n2);
+    return v(a.x / n, a.y / n, a.z / n);
+}
+
+// (1 - t) a + t b, each product and the sum rounded on its own.
+KHS_HD V glerp(V a, V b, double t)
+{
+    const double u = xs(1.0, t);
+    return v(xa(xm(a.x, u), xm(b.x, t)), xa(xm(a.y, u), xm(b.y, t)), xa(xm(a.z, u), xm(b.z, t)));
+}
+
+// Frame (row-major, columns d1 d2 d3) from d3 = the normalised tangent and
+// d1 the hint made orthogonal to it (math.hpp:26-43).
+KHS_HD M frame_from_d3(V d3, V hint)
+{
+    V d1 = gsub(hint, gmul(d3, gdot(hint, d3)));
+    if (gdot(d1, d1) < 1.0e-16) {
+        const V axis = fabs(d3.x) < 0.8 ? v(1.0, 0.0, 0.0) : v(0.0, 1.0, 0.0);
+        d1 = gsub(axis, gmul(d3, gdot(axis, d3)));
+    }
+    d1 = gunit(d1);
+    const V d2 = gunit(gcross(d3, d1));
+    d1 = gunit(gcross(d2, d3));
+    M r;
+    r.m[0] = d1.x; r.m[1] = d2.x; r.m[2] = d3.x;
+    r.m[3] = d1.y; r.m[4] = d2.y; r.m[5] = d3.y;
+    r.m[6] = d1.z; r.m[7] = d2.z; r.m[8] = d3.z;
+    return r;
+}
+
+KHS_HD M frame_from_tangent(V tangent, V hint) { return frame_from_d3(gunit(tangent), hint); }
+
+// A unit vector orthogonal to s, chosen like Eigen's unitOrthogonal.
+KHS_HD V unit_orthogonal(V s)
+{
+    const double eps = 1e-12;
+    if (!(fabs(s.x) <= xm(fabs(s.z), eps)) || !(fabs(s.y) <= xm(fabs(s.z), eps))) {
+        const double inv = 1.0 / sqrt(xa(xm(s.x, s.x), xm(s.y, s.y)));
+        return v(xm(-s.y, inv), xm(s.x, inv), 0.0);
+    }
+    const double inv = 1.0 / sqrt(xa(xm(s.y, s.y), xm(s.z, s.z)));
+    return v(0.0, xm(-s.z, inv), xm(s.y, inv));
+}
+
+// The minimal rotation taking `from` to `to` (math.hpp:45-58), split into
+// the part that depends on the two tangents only and its application to a
+// director: Rodrigues' formula about n = from x to / |from x to| (kind 0),
+// the identity for parallel tangents (kind 1), a half turn about an
+// orthogonal axis n for opposite ones (kind 2).
+struct Transport {
+    V n;
+    double s, c;
+    int kind;
+};
+
+KHS_HD Transport transport_between(V from, V to)
+{
+    const V a = gunit(from), b = gunit(to);
+    const V axis = gcross(a, b);
+    Transport t;
+    t.s = sqrt(gdot(axis, axis));
+    const double c = gdot(a, b);
+    t.c = c < -1.0 ? -1.0 : (1.0 < c ? 1.0 : c);
+    t.kind = 0;
+    if (t.s < 1.0e-12) {
+        t.kind = t.c > 0.0 ? 1 : 2;
+        t.n = t.kind == 2 ? unit_orthogonal(a) : v(0.0, 0.0, 0.0);
+    } else {
+        t.n = v(axis.x / t.s, axis.y / t.s, axis.z / t.s);
+    }
+    return t;
+}
+
+KHS_HD V transport_apply(const Transport &t, V director)
+{
+    if (t.kind == 1) return director;
+    if (t.kind == 2) return gsub(gmul(gmul(t.n, 2.0), gdot(t.n, director)), director);
+    return gadd(gadd(gmul(director, t.c), gmul(gcross(t.n, director), t.s)), gmul(gmul(t.n, gdot(t.n, director)), xs(1.0, t.c)));
+}
+
+KHS_HD V parallel_transport(V director, V from, V to) { return transport_apply(transport_between(from, to), director); }
+
+// a * b^T for row-major 3x3 matrices.
+KHS_HD M times_transpose(const M &a, const M &b)
+{
+    M r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            r.m[3 * i + j] = xa(xa(xm(a.m[3 * i], b.m[3 * j]), xm(a.m[3 * i + 1], b.m[3 * j + 1])), xm(a.m[3 * i + 2], b.m[3 * j + 2]));
+    return r;
+}
+
+// Rotation vector (axis * angle, angle in (-pi, pi]) of a rotation matrix:
+// the quaternion from the largest of its four squared components, then
+// angle = 2 atan2(|v|, |w|) with the axis carrying the sign of w.
+KHS_HD V rotation_vector(const M &r)
+{
+    double q[4];  // x y z w
+    const double tr = xa(xa(r.m[0], r.m[4]), r.m[8]);
+    if (tr > 0.0) {
+        double s = sqrt(xa(tr, 1.0));
+        q[3] = xm(0.5, s);
+        s = 0.5 / s;
+        q[0] = xm(xs(r.m[7], r.m[5]), s);
+        q[1] = xm(xs(r.m[2], r.m[6]), s);
+        q[2] = xm(xs(r.m[3], r.m[1]), s);
+    } else {
+        int i = 0;
+        if (r.m[4] > r.m[0]) i = 1;
+        if (r.m[8] > r.m[4 * i]) i = 2;
+        const int j = (i + 1) % 3, k = (j + 1) % 3;
+        double s = sqrt(xa(xs(xs(r.m[4 * i], r.m[4 * j]), r.m[4 * k]), 1.0));
+        q[i] = xm(0.5, s);
+        s = 0.5 / s;
+        q[3] = xm(xs(r.m[3 * k + j], r.m[3 * j + k]), s);
+        q[j] = xm(xa(r.m[3 * j + i], r.m[3 * i + j]), s);
+        q[k] = xm(xa(r.m[3 * k + i], r.m[3 * i + k]), s);
+    }
+    double n = sqrt(xa(xa(xm(q[0], q[0]), xm(q[1], q[1])), xm(q[2], q[2])));
+    if (!(n != 0.0)) return v(0.0, 0.0, 0.0);
+    double angle = xm(2.0, atan2(n, fabs(q[3])));
+    if (q[3] < 0.0) n = -n;
+    const V axis = v(q[0] / n, q[1] / n, q[2] / n);
+    if (!gfinite(angle) || !gfinite(axis.x) || !gfinite(axis.y) || !gfinite(axis.z)) return v(0.0, 0.0, 0.0);
+    if (angle > kPi) angle = xs(angle, xm(2.0, kPi));
+    return gmul(axis, angle);
+}
+
 }  // namespace dm
 }  // namespace khs

@@ -31,6 +31,9 @@
 //                 k_steepest, k_scale, k_reduce_dir, k_final_dir
 //   CCD           k_ccd (plain), k_ccd_collect + k_ccd_pairs (mixed)
 //   queries       k_contact, k_contact_query_records, k_gather
+//   root targets  k_root_tangents, k_root_transport, k_root_frames (thread
+//                 per strand), k_root_rotations: per call of
+//                 khsUpdateRootTargets / khsSetRootAnimationFrame
 // Reductions are two-level (fixed per-block trees, then one block over the
 // partials) and therefore deterministic.
 #include "khs_engine.hpp"
@@ -2365,6 +2368,96 @@ __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32
     out[3 * size_t(i) + 2] = q[6 * size_t(n) + 2];
 }
 
+// ---- root targets (src/solver.cpp:416-447) --------------------------------
+//
+// Target positions and rotation vectors of every node for one set of
+// evaluated source points: positions and unit tangents, the tangent-only
+// part of each frame step (thread per node), the frame walk along each
+// strand (thread per strand, longest strands first), then the rotation
+// vector of frame * reference^T (thread per node).
+
+struct RootArgs {
+    uint32_t N, S;
+    const double *points;                    // [P][3] evaluated source points
+    const uint32_t *bind_l, *bind_r;         // the two source points a node interpolates
+    const double *bind_t;
+    const uint32_t *node_strand, *sfirst, *scount, *sorder;
+    const double *ref;                       // [N][9] reference frames
+    double *x, *tangent, *frame, *rot;       // [N][3], [N][3], [N][9], [N][3]
+    uint32_t *bad;                           // nonzero after a degenerate tangent
+};
+
+__device__ __forceinline__ V root_position(const RootArgs &a, uint32_t n)
+{
+    return dm::glerp(load3(a.points + 3 * size_t(a.bind_l[n])), load3(a.points + 3 * size_t(a.bind_r[n])), a.bind_t[n]);
+}
+
+// Central-difference tangents, one-sided at the strand ends
+// (solver.cpp:426-433); a squared length below 1e-24 fails the whole call.
+__global__ void __launch_bounds__(kBlock) k_root_tangents(RootArgs a)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.N) return;
+    const uint32_t s = a.node_strand[n], k = n - a.sfirst[s], count = a.scount[s];
+    const V x = root_position(a, n);
+    store3(a.x + 3 * size_t(n), x);
+    V d;
+    if (k == 0) d = dm::gsub(root_position(a, n + 1), x);
+    else if (k + 1 == count) d = dm::gsub(x, root_position(a, n - 1));
+    else d = dm::gsub(root_position(a, n + 1), root_position(a, n - 1));
+    if (dm::gdot(d, d) < 1.0e-24) atomicOr(a.bad, 1u);
+    store3(a.tangent + 3 * size_t(n), dm::gunit(d));
+}
+
+// Everything of the frame walk that depends on the tangents alone, per node:
+// d3 (the tangent normalised once more, as frame_from_tangent does) and the
+// minimal rotation from the previous node's tangent, packed into the node's
+// frame slot [d3, n, s, c, kind] until k_root_frames replaces it.
+__global__ void __launch_bounds__(kBlock) k_root_transport(RootArgs a)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.N) return;
+    const V t = load3(a.tangent + 3 * size_t(n));
+    double *p = a.frame + 9 * size_t(n);
+    store3(p, dm::gunit(t));
+    dm::Transport tr{};
+    tr.kind = 1;
+    if (n != a.sfirst[a.node_strand[n]]) tr = dm::transport_between(load3(a.tangent + 3 * size_t(n - 1)), t);
+    store3(p + 3, tr.n);
+    p[6] = tr.s; p[7] = tr.c; p[8] = double(tr.kind);
+}
+
+// The sequential part (solver.cpp:435-443): each frame's first column is the
+// previous one carried by the minimal rotation between consecutive tangents.
+// One thread per strand, longest strands first.
+__global__ void __launch_bounds__(kBlock) k_root_frames(RootArgs a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.S) return;
+    const uint32_t s = a.sorder[i], first = a.sfirst[s], count = a.scount[s];
+    const double *r0 = a.ref + 9 * size_t(first);
+    double *p = a.frame + 9 * size_t(first);
+    M f = dm::frame_from_d3(load3(p), dm::v(r0[0], r0[3], r0[6]));
+#pragma unroll
+    for (int c = 0; c < 9; ++c) p[c] = f.m[c];
+    for (uint32_t k = 1; k < count; ++k) {
+        p += 9;
+        dm::Transport tr;
+        tr.n = load3(p + 3); tr.s = p[6]; tr.c = p[7]; tr.kind = int(p[8]);
+        f = dm::frame_from_d3(load3(p), dm::transport_apply(tr, dm::v(f.m[0], f.m[3], f.m[6])));
+#pragma unroll
+        for (int c = 0; c < 9; ++c) p[c] = f.m[c];
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_root_rotations(RootArgs a)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.N) return;
+    const M r = dm::times_transpose(load9(a.frame + 9 * size_t(n)), load9(a.ref + 9 * size_t(n)));
+    store3(a.rot + 3 * size_t(n), dm::rotation_vector(r));
+}
+
 // ---- device memory --------------------------------------------------------
 
 struct Arena {
@@ -2401,6 +2494,14 @@ struct Engine::Impl {
     double *anim_root_x = nullptr, *anim_root_r = nullptr, *anim_col = nullptr;
     size_t anim_bytes = 0, ring_bytes = 0;
     double *col_a_copy = nullptr;  // frame-start copy used while stepping
+    // Root targets on the device: the two source points each node
+    // interpolates and its strand (arena), and the work arrays of one pass
+    // (allocated on first use: points [P][3], positions, tangents, frames,
+    // rotation vectors, the degenerate-tangent flag).
+    uint32_t *bind_l = nullptr, *bind_r = nullptr, *node_strand = nullptr;
+    double *bind_t = nullptr;
+    char *root_work = nullptr;
+    RootArgs root{};
     std::vector<uint8_t> fixed_host;
     uint64_t resident = 0;
 
@@ -2472,6 +2573,7 @@ struct Engine::Impl {
         if (arena.base) cudaFree(arena.base);
         if (ring) cudaFree(ring);
         if (anim_root_x) cudaFree(anim_root_x);
+        if (root_work) cudaFree(root_work);
         if (mail_host) cudaFreeHost(mail_host);
         if (sweep_host) cudaFreeHost(sweep_host);
         if (ev_begin) cudaEventDestroy(ev_begin);
@@ -2514,6 +2616,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     bytes += 2 * padded<double>(3 * N);      // as_i_f as_j_f
     bytes += padded<uint8_t>(N) + 2 * padded<int32_t>(N);
     bytes += 4 * padded<double>(3 * N);      // root cur/pending x r
+    bytes += 3 * padded<uint32_t>(N) + padded<double>(N);  // root bindings, node strand
     bytes += 3 * padded<uint32_t>(E) + padded<uint8_t>(E) + padded<double>(E) + 2 * padded<double>(3 * E);
     bytes += 3 * padded<double>(E) + 2 * padded<uint32_t>(E) + padded<uint8_t>(E);
     bytes += 4 * padded<uint32_t>(S);
@@ -2556,6 +2659,8 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     int32_t *eleft = a.take<int32_t>(N), *eright = a.take<int32_t>(N);
     I.root_cur_x = a.take<double>(3 * N); I.root_cur_r = a.take<double>(3 * N);
     I.root_pend_x = a.take<double>(3 * N); I.root_pend_r = a.take<double>(3 * N);
+    I.bind_l = a.take<uint32_t>(N); I.bind_r = a.take<uint32_t>(N); I.node_strand = a.take<uint32_t>(N);
+    I.bind_t = a.take<double>(N);
     uint32_t *ei = a.take<uint32_t>(E), *ej = a.take<uint32_t>(E), *es = a.take<uint32_t>(E);
     uint8_t *ec = a.take<uint8_t>(E);
     double *L0 = a.take<double>(E), *g0 = a.take<double>(3 * E), *k0 = a.take<double>(3 * E);
@@ -2631,6 +2736,14 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     up(eleft, hl.data(), N * 4); up(eright, hr.data(), N * 4);
     up(I.root_cur_x, hrx.data(), 3 * N * 8); up(I.root_cur_r, hrr.data(), 3 * N * 8);
     up(I.root_pend_x, hrx.data(), 3 * N * 8); up(I.root_pend_r, hrr.data(), 3 * N * 8);
+    std::vector<uint32_t> hbl(N), hbr(N);
+    std::vector<double> hbt(N);
+    for (size_t n = 0; n < N; ++n) { hbl[n] = m.binding[n].left; hbr[n] = m.binding[n].right; hbt[n] = m.binding[n].t; }
+    up(I.bind_l, hbl.data(), N * 4); up(I.bind_r, hbr.data(), N * 4); up(I.bind_t, hbt.data(), N * 8);
+    up(I.node_strand, m.node_strand.data(), N * 4);
+    I.root.N = uint32_t(N); I.root.S = uint32_t(S);
+    I.root.bind_l = I.bind_l; I.root.bind_r = I.bind_r; I.root.bind_t = I.bind_t; I.root.node_strand = I.node_strand;
+    I.root.sfirst = sf; I.root.scount = sc; I.root.sorder = so; I.root.ref = ref;
     up(ei, m.elem_i.data(), E * 4); up(ej, m.elem_j.data(), E * 4); up(es, m.elem_strand.data(), E * 4);
     up(ec, m.elem_contact.data(), E);
     up(L0, m.rest_length.data(), E * 8); up(g0, hg0.data(), 3 * E * 8); up(k0, hk0.data(), 3 * E * 8);
@@ -2714,18 +2827,63 @@ void Engine::update_runtime(const KhsSolverDesc &desc, const KhsHairMaterial &ma
     trust_radius_ = std::fmax(0.25 * max_rest_length_, 8.0 * (material.radius + material.collider_offset + material.barrier_distance));
 }
 
-void Engine::set_pending_roots(const std::vector<Vec> &pos, const std::vector<Vec> &rot)
+KhsResult Engine::run_root_pass(const KhsVec3 *points, uint32_t count)
 {
     Impl &I = *d_;
     const size_t N = I.v.N;
-    std::vector<double> x(3 * N), r(3 * N);
-    for (size_t n = 0; n < N; ++n) {
-        x[3 * n] = pos[n].x; x[3 * n + 1] = pos[n].y; x[3 * n + 2] = pos[n].z;
-        r[3 * n] = rot[n].x; r[3 * n + 1] = rot[n].y; r[3 * n + 2] = rot[n].z;
+    if (!points || count != I.original_count) return fail(KHS_ERROR_INVALID_ARGUMENT, "the root target point count does not match the source curves");
+    if (!I.root_work) {
+        const size_t bytes = padded<double>(3 * size_t(count)) + 3 * padded<double>(3 * N) + padded<double>(9 * N) +
+                             padded<uint32_t>(1);
+        char *base = nullptr;
+        if (cudaMalloc(reinterpret_cast<void **>(&base), bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(KHS_ERROR_OUT_OF_MEMORY, "cannot allocate the device root-target arrays");
+        }
+        I.root_work = base;
+        I.resident += bytes;
+        gpu_stats_.resident_bytes = I.resident;
+        size_t off = 0;
+        auto take = [&](size_t doubles) { double *p = reinterpret_cast<double *>(base + off); off += padded<double>(doubles); return p; };
+        I.root.points = take(3 * size_t(count));
+        I.root.x = take(3 * N); I.root.tangent = take(3 * N); I.root.rot = take(3 * N); I.root.frame = take(9 * N);
+        I.root.bad = reinterpret_cast<uint32_t *>(base + off);
     }
-    KHS_CUDA(cudaMemcpyAsync(I.root_pend_x, x.data(), x.size() * 8, cudaMemcpyHostToDevice, I.stream));
-    KHS_CUDA(cudaMemcpyAsync(I.root_pend_r, r.data(), r.size() * 8, cudaMemcpyHostToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(const_cast<double *>(I.root.points), points, size_t(count) * 24, cudaMemcpyHostToDevice, I.stream));
+    KHS_CUDA(cudaMemsetAsync(I.root.bad, 0, sizeof(uint32_t), I.stream));
+    I.launch("k_root_tangents", k_root_tangents, grid_for(N), kBlock, I.root);
+    I.launch("k_root_transport", k_root_transport, grid_for(N), kBlock, I.root);
+    I.launch("k_root_frames", k_root_frames, grid_for(I.v.S), kBlock, I.root);
+    I.launch("k_root_rotations", k_root_rotations, grid_for(N), kBlock, I.root);
+    I.check();
+    uint32_t bad = 0;
+    KHS_CUDA(cudaMemcpyAsync(&bad, I.root.bad, sizeof(bad), cudaMemcpyDeviceToHost, I.stream));
     I.sync();
+    if (bad) return fail(KHS_ERROR_INVALID_HAIR, "cannot compute root directions from the root targets");
+    return KHS_OK;
+}
+
+KhsResult Engine::set_pending_root_points(const KhsVec3 *points, uint32_t count)
+{
+    Impl &I = *d_;
+    const KhsResult r = run_root_pass(points, count);
+    if (r != KHS_OK) return r;
+    const size_t bytes = 3 * size_t(I.v.N) * 8;
+    KHS_CUDA(cudaMemcpyAsync(I.root_pend_x, I.root.x, bytes, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.root_pend_r, I.root.rot, bytes, cudaMemcpyDeviceToDevice, I.stream));
+    return KHS_OK;
+}
+
+KhsResult Engine::root_targets_to_host(const KhsVec3 *points, uint32_t count, KhsVec3 *positions, KhsVec3 *rotations)
+{
+    Impl &I = *d_;
+    const KhsResult r = run_root_pass(points, count);
+    if (r != KHS_OK) return r;
+    const size_t bytes = 3 * size_t(I.v.N) * 8;
+    KHS_CUDA(cudaMemcpyAsync(positions, I.root.x, bytes, cudaMemcpyDeviceToHost, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(rotations, I.root.rot, bytes, cudaMemcpyDeviceToHost, I.stream));
+    I.sync();
+    return KHS_OK;
 }
 
 void Engine::set_pending_collider(const std::vector<Vec> &vertices)
@@ -2762,15 +2920,17 @@ KhsResult Engine::allocate_animation(uint32_t frames)
     return KHS_OK;
 }
 
-KhsResult Engine::set_root_animation_frame(uint32_t frame, const std::vector<Vec> &pos, const std::vector<Vec> &rot)
+KhsResult Engine::set_root_animation_frame(uint32_t frame, const KhsVec3 *points, uint32_t count)
 {
     Impl &I = *d_;
     const size_t N = I.v.N;
-    if (frame >= animation_frames_ || pos.size() != N || rot.size() != N)
-        return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid root animation frame");
-    KHS_CUDA(cudaMemcpyAsync(I.anim_root_x + size_t(frame) * 3 * N, pos.data(), 3 * N * 8, cudaMemcpyHostToDevice, I.stream));
-    KHS_CUDA(cudaMemcpyAsync(I.anim_root_r + size_t(frame) * 3 * N, rot.data(), 3 * N * 8, cudaMemcpyHostToDevice, I.stream));
-    I.sync();
+    // Targets first, then the frame index, in the reference's order
+    // (solver.cpp:802-824 computes before the backend checks the frame).
+    const KhsResult r = run_root_pass(points, count);
+    if (r != KHS_OK) return r;
+    if (frame >= animation_frames_) return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid root animation frame");
+    KHS_CUDA(cudaMemcpyAsync(I.anim_root_x + size_t(frame) * 3 * N, I.root.x, 3 * N * 8, cudaMemcpyDeviceToDevice, I.stream));
+    KHS_CUDA(cudaMemcpyAsync(I.anim_root_r + size_t(frame) * 3 * N, I.root.rot, 3 * N * 8, cudaMemcpyDeviceToDevice, I.stream));
     root_frame_set_[frame] = true;
     return KHS_OK;
 }

@@ -42,11 +42,17 @@ public:
                     const std::vector<Vec> &root_pos, const std::vector<Vec> &root_rot);
     void update_runtime(const KhsSolverDesc &desc, const KhsHairMaterial &material, const std::vector<double> &mass,
                         const std::vector<double> &rotational_mass);
-    void set_pending_roots(const std::vector<Vec> &pos, const std::vector<Vec> &rot);
+    // Root targets of every node (positions and rotation vectors) for the
+    // evaluated source points, computed on the device (solver.cpp:416-447):
+    // into the pending targets of the next step, into an animation frame, or
+    // back to the host.  The points must be finite; a degenerate tangent
+    // gives KHS_ERROR_INVALID_HAIR and changes nothing.
+    KhsResult set_pending_root_points(const KhsVec3 *points, uint32_t count);
+    KhsResult root_targets_to_host(const KhsVec3 *points, uint32_t count, KhsVec3 *positions, KhsVec3 *rotations);
     void set_pending_collider(const std::vector<Vec> &vertices);
 
     KhsResult allocate_animation(uint32_t frames);
-    KhsResult set_root_animation_frame(uint32_t frame, const std::vector<Vec> &pos, const std::vector<Vec> &rot);
+    KhsResult set_root_animation_frame(uint32_t frame, const KhsVec3 *points, uint32_t count);
     KhsResult set_collider_animation_frame(uint32_t frame, const KhsVec3 *vertices, uint32_t count);
     KhsResult finalize_animation();
 
@@ -99,6 +105,7 @@ private:
     std::unique_ptr<Impl> d_;
 
     KhsResult fail(KhsResult r, const std::string &message);
+    KhsResult run_root_pass(const KhsVec3 *points, uint32_t count);
     void clear_failure();
     void set_failure_context(uint32_t kind, uint32_t frame, uint32_t sub, uint32_t attempted, uint32_t maximum,
                              uint32_t attempts);

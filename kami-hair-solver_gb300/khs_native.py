@@ -209,6 +209,7 @@ EXTENSION_FUNCTIONS = [
     ("khsxSetRollbackRing", ctypes.c_int, [VP, c_u32]),
     ("khsxRollbackToFrame", ctypes.c_int, [VP, c_u32]),
     ("khsxQueryContactsNoAlloc", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
+    ("khsxComputeRootTargets", ctypes.c_int, [VP, VP, c_u32, VP, VP, c_u32]),
     ("khsxSetProfiling", ctypes.c_int, [VP, c_u32]),
     ("khsxGetKernelTimings", c_u32, [VP, VP, c_u32]),
     ("khsxResetKernelTimings", ctypes.c_int, [VP]),
@@ -498,6 +499,16 @@ class HairSolver:
         if out.dtype != CONTACT_DTYPE or not out.flags.c_contiguous:
             raise ValueError("out must be a contiguous CONTACT_DTYPE array")
         return int(self._library.khsxQueryContactsNoAlloc(self._handle, _ptr(q), q.size, _ptr(out), out.size))
+
+    def compute_root_targets(self, points) -> tuple[np.ndarray, np.ndarray]:
+        """khsxComputeRootTargets: (positions, rotation vectors) of every
+        internal node, each (N, 3), for the evaluated source points."""
+        pts = _vec3_buffer(points)
+        n = self.build_stats().internal_node_count
+        pos = np.zeros((n, 3), dtype=np.float64)
+        rot = np.zeros((n, 3), dtype=np.float64)
+        self._check(self._library.khsxComputeRootTargets(self._handle, _ptr(pts), len(pts), _ptr(pos), _ptr(rot), n))
+        return pos, rot
 
     def contact_records(self) -> np.ndarray:
         count = self.build_stats().element_count

@@ -570,6 +570,26 @@ public:
         return KHS_OK;
     }
 
+    // Extension khsxComputeRootTargets: the targets update_roots computes,
+    // copied out instead of stored.
+    KhsResult roots_to_host(const KhsVec3 *p, uint32_t n, KhsVec3 *pos_out, KhsVec3 *rot_out, uint32_t capacity)
+    {
+        if (!built_ || !p || n != input_points_.size()) { error_ = "root target count mismatch"; return KHS_ERROR_INVALID_ARGUMENT; }
+        std::vector<V3> conv(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            conv[i] = v3(p[i].x, p[i].y, p[i].z);
+            if (!finite3(conv[i])) { error_ = "non-finite root target"; return KHS_ERROR_INVALID_HAIR; }
+        }
+        if (!pos_out || !rot_out || capacity < N()) { error_ = "root target output too small"; return KHS_ERROR_INVALID_ARGUMENT; }
+        std::vector<V3> pos, rot;
+        if (!compute_root_targets(conv, pos, rot)) { error_ = "cannot compute root directions"; return KHS_ERROR_INVALID_HAIR; }
+        for (size_t k = 0; k < N(); ++k) {
+            pos_out[k] = {pos[k].x, pos[k].y, pos[k].z};
+            rot_out[k] = {rot[k].x, rot[k].y, rot[k].z};
+        }
+        return KHS_OK;
+    }
+
     KhsResult step(double frame_dt)
     {
         if (!built_) { error_ = "prepare the solver first"; return KHS_ERROR_INVALID_STATE; }
@@ -2051,6 +2071,8 @@ KHS_API uint32_t khsxGetSubstepRecordCount(const KhsSolver *s) { return s ? s->i
 KHS_API KhsResult khsxCopySubstepRecords(const KhsSolver *s, KhsxSubstepRecord *r, uint32_t c) { return s ? s->impl.copy_records(r, c) : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API KhsResult khsxCopyContactRecords(const KhsSolver *s, KhsxContactRecord *r, uint32_t c) { return s ? s->impl.copy_contacts(r, c) : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API KhsResult khsxQueryContacts(KhsSolver *s, const double *q, uint64_t n, KhsxContactRecord *r, uint32_t c) { return s ? s->impl.query_contacts(q, n, r, c) : KHS_ERROR_INVALID_ARGUMENT; }
+KHS_API KhsResult khsxComputeRootTargets(KhsSolver *s, const KhsVec3 *p, uint32_t n, KhsVec3 *pos, KhsVec3 *rot, uint32_t cap)
+{ return guarded(s, [&] { return s->impl.roots_to_host(p, n, pos, rot, cap); }); }
 
 // Oracle-only test hook (see Solver::export_system).
 KHS_API void khsOracleExportSystem(const KhsSolver *s, double *diag, double *upper, double *grad, uint32_t *strands)
