@@ -308,26 +308,86 @@ double segment_triangle_distance(Vec p0, Vec p1, Vec a, Vec b, Vec c)
     return best;
 }
 
-bool inside_closed(const Model &m, Vec p)
+// Whether the ray p + t (1, 1.2345e-6, 2.3456e-6), t > 1e-12, crosses the
+// triangle: the per-triangle test of the reference's ray-parity inside test
+// (solver.cpp:608-632), Moller-Trumbore with its thresholds.
+constexpr double kRayDy = 0.0000012345, kRayDz = 0.0000023456;
+
+inline bool ray_crosses(Vec p, Vec a, Vec b, Vec c)
 {
-    uint32_t hits = 0;
-    const Vec dir = mk(1.0, 0.0000012345, 0.0000023456);
-    for (size_t t = 0; t < m.tri.size() / 3; ++t) {
-        const Vec a = m.collider[m.tri[3 * t]], b = m.collider[m.tri[3 * t + 1]], c = m.collider[m.tri[3 * t + 2]];
-        const Vec e1 = sub(b, a), e2 = sub(c, a), h = cross(dir, e2);
-        const double det = dot(e1, h);
-        if (std::fabs(det) < 1.0e-14) continue;
-        const double inv = 1.0 / det;
-        const Vec s = sub(p, a);
-        const double u = inv * dot(s, h);
-        if (u < 0.0 || u > 1.0) continue;
-        const Vec q = cross(s, e1);
-        const double v = inv * dot(dir, q);
-        if (v < 0.0 || u + v > 1.0) continue;
-        if (inv * dot(e2, q) > 1.0e-12) ++hits;
-    }
-    return (hits & 1u) != 0;
+    const Vec dir = mk(1.0, kRayDy, kRayDz);
+    const Vec e1 = sub(b, a), e2 = sub(c, a), h = cross(dir, e2);
+    const double det = dot(e1, h);
+    if (std::fabs(det) < 1.0e-14) return false;
+    const double inv = 1.0 / det;
+    const Vec s = sub(p, a);
+    const double u = inv * dot(s, h);
+    if (u < 0.0 || u > 1.0) return false;
+    const Vec q = cross(s, e1);
+    const double v = inv * dot(dir, q);
+    if (v < 0.0 || u + v > 1.0) return false;
+    return inv * dot(e2, q) > 1.0e-12;
 }
+
+// The reference loops over every triangle per point (O(points x
+// triangles): minutes for a 1.8M-node request on a 20k-triangle body).  Here
+// a host BVH skips triangles that loop cannot count, and the hit count is
+// otherwise the same test on the same values, so the parity is identical:
+//   a counted triangle's exact ray-plane point Q lies within `pad` of the
+//   triangle (the rounding of its barycentric test is at most about
+//   0.1 E^2 (S + 2E) with E the longest edge and S the scene diagonal, since
+//   |det| >= 1e-14; `pad` takes 20 times that), at a ray parameter above
+//   -pad; the walk visits every node whose box grown by `pad` the ray
+//   crosses for x >= p.x - pad, which includes Q's leaf.
+struct InsideTester {
+    const Model &m;
+    TreeBuilder tb;
+    double pad = 0.0;
+
+    // `points`: every point that will be tested (they bound S).
+    InsideTester(const Model &model, const std::vector<Vec> &points) : m(model), tb{model.collider, model.tri, false, {}, {}}
+    {
+        tb.run();
+        double edge2 = 0.0;
+        for (size_t t = 0; t < m.tri.size() / 3; ++t)
+            for (int e = 0; e < 3; ++e)
+                edge2 = std::max(edge2, sq(sub(m.collider[m.tri[3 * t + e]], m.collider[m.tri[3 * t + (e + 1) % 3]])));
+        Vec lo = mk(1e300, 1e300, 1e300), hi = mk(-1e300, -1e300, -1e300);
+        for (const Vec &v : m.collider) { lo = vmin(lo, v); hi = vmax(hi, v); }
+        for (const Vec &v : points) { lo = vmin(lo, v); hi = vmax(hi, v); }
+        const double scene = points.empty() && m.collider.empty() ? 0.0 : len(sub(hi, lo));
+        const double edge = std::sqrt(edge2);
+        pad = 2.0 * edge2 * (scene + 2.0 * edge) + 1.0e-9;
+    }
+
+    // The ray meets the box grown by pad at some x >= p.x - pad.
+    bool ray_meets(Vec p, const TreeNode &nd) const
+    {
+        const double x0 = std::max(nd.lo.x, p.x) - pad, x1 = nd.hi.x + pad;
+        if (x1 < x0) return false;
+        const double y0 = p.y + (x0 - p.x) * kRayDy, y1 = p.y + (x1 - p.x) * kRayDy;
+        const double z0 = p.z + (x0 - p.x) * kRayDz, z1 = p.z + (x1 - p.x) * kRayDz;
+        return y1 >= nd.lo.y - pad && y0 <= nd.hi.y + pad && z1 >= nd.lo.z - pad && z0 <= nd.hi.z + pad;
+    }
+
+    bool inside(Vec p, std::vector<int> &stack) const
+    {
+        if (tb.nodes.empty()) return false;
+        uint32_t hits = 0;
+        stack.assign(1, 0);
+        while (!stack.empty()) {
+            const TreeNode &nd = tb.nodes[stack.back()];
+            stack.pop_back();
+            if (!ray_meets(p, nd)) continue;
+            if (nd.left >= 0) { stack.push_back(nd.left); stack.push_back(nd.right); continue; }
+            for (uint32_t k = nd.begin; k < nd.begin + nd.count; ++k) {
+                const uint32_t t = tb.order[k];
+                if (ray_crosses(p, m.collider[m.tri[3 * t]], m.collider[m.tri[3 * t + 1]], m.collider[m.tri[3 * t + 2]])) ++hits;
+            }
+        }
+        return (hits & 1u) != 0;
+    }
+};
 
 }  // namespace
 
@@ -546,16 +606,19 @@ double minimum_gap_host(const Model &m, const KhsHairMaterial &material, uint64_
 bool initial_feasibility(const Model &m, const KhsSolverDesc &desc, const KhsHairMaterial &material,
                          double &minimum_gap, std::string &error)
 {
-    if (m.closed_manifold)
+    if (m.closed_manifold) {
+        const InsideTester tester(m, m.x);
+        std::vector<int> stack;
         for (size_t k = 0; k < m.nodes(); ++k) {
             if (m.fixed[k] || m.virtual_extension[k]) continue;
-            if (inside_closed(m, m.x[k])) {
+            if (tester.inside(m.x[k], stack)) {
                 std::ostringstream ss;
                 ss << "initial intersection: internal node " << k << " lies inside the closed collider";
                 error = ss.str();
                 return false;
             }
         }
+    }
     uint64_t candidates = 0;
     minimum_gap = minimum_gap_host(m, material, &candidates);
     if (minimum_gap <= desc.minimum_gap) {
@@ -566,6 +629,14 @@ bool initial_feasibility(const Model &m, const KhsSolverDesc &desc, const KhsHai
         return false;
     }
     return true;
+}
+
+void inside_closed_collider(const Model &m, const std::vector<Vec> &points, std::vector<uint8_t> &inside)
+{
+    inside.assign(points.size(), 0);
+    const InsideTester tester(m, points);
+    std::vector<int> stack;
+    for (size_t k = 0; k < points.size(); ++k) inside[k] = tester.inside(points[k], stack) ? 1 : 0;
 }
 
 void build_device_bvh(Model &m)

@@ -115,6 +115,11 @@ void collider_topology(Model &model);
 bool initial_feasibility(const Model &model, const KhsSolverDesc &desc, const KhsHairMaterial &material,
                          double &minimum_gap, std::string &error);
 
+// Ray-parity inside flags of points against the collider, with the
+// reference's per-triangle test and parity rule (solver.cpp:608-632) walked
+// over a host BVH; the same flags as the reference's all-triangle loop.
+void inside_closed_collider(const Model &model, const std::vector<Vec> &points, std::vector<uint8_t> &inside);
+
 // Minimum gap of contact-enabled elements (solver.cpp:659-681).
 double minimum_gap_host(const Model &model, const KhsHairMaterial &material, uint64_t *candidates);
 

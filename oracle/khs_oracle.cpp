@@ -1069,21 +1069,8 @@ private:
     bool point_inside(V3 p) const
     {
         uint32_t hits = 0;
-        const V3 dir = v3(1.0, 0.0000012345, 0.0000023456);
-        for (const Tri &t : triangles_) {
-            const V3 a = collider_current_[t.i0], b = collider_current_[t.i1], c = collider_current_[t.i2];
-            const V3 e1 = b - a, e2 = c - a, h = cross(dir, e2);
-            const double det = dot(e1, h);
-            if (std::fabs(det) < 1.0e-14) continue;
-            const double inv = 1.0 / det;
-            const V3 s = p - a;
-            const double u = inv * dot(s, h);
-            if (u < 0.0 || u > 1.0) continue;
-            const V3 q = cross(s, e1);
-            const double v = inv * dot(dir, q);
-            if (v < 0.0 || u + v > 1.0) continue;
-            if (inv * dot(e2, q) > 1.0e-12) ++hits;
-        }
+        for (const Tri &t : triangles_)
+            if (ray_crosses_triangle(p, collider_current_[t.i0], collider_current_[t.i1], collider_current_[t.i2])) ++hits;
         return (hits & 1u) != 0;
     }
 

@@ -107,6 +107,25 @@ inline V3 unit_orthogonal(V3 s)
     return v3(0.0, -s.z * inv, s.y * inv);
 }
 
+// One triangle of the ray-parity inside test (solver.cpp:608-632): whether
+// the ray p + t (1, 1.2345e-6, 2.3456e-6), t > 1e-12, crosses the triangle
+// (Moller-Trumbore with the reference's thresholds).
+inline bool ray_crosses_triangle(V3 p, V3 a, V3 b, V3 c)
+{
+    const V3 dir = v3(1.0, 0.0000012345, 0.0000023456);
+    const V3 e1 = b - a, e2 = c - a, h = cross(dir, e2);
+    const double det = dot(e1, h);
+    if (std::fabs(det) < 1.0e-14) return false;
+    const double inv = 1.0 / det;
+    const V3 s = p - a;
+    const double u = inv * dot(s, h);
+    if (u < 0.0 || u > 1.0) return false;
+    const V3 q = cross(s, e1);
+    const double v = inv * dot(dir, q);
+    if (v < 0.0 || u + v > 1.0) return false;
+    return inv * dot(e2, q) > 1.0e-12;
+}
+
 // Orthonormal frame whose third column is the tangent (math.hpp:26-43).
 inline M3 frame_from_tangent(V3 tangent, V3 hint)
 {
