@@ -40,6 +40,7 @@
 #include "khs_device_math.cuh"
 #include "khs_ff.cuh"
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -97,6 +98,7 @@ struct Scalars {
     uint32_t refine_bits; // largest relative refinement correction (FP32 bits)
     uint32_t near_count;  // elements queued for the warp-cooperative contact pass
     uint32_t ccd_near;    // elements queued for the warp-cooperative CCD pass
+    uint32_t pool_used;   // entries of the leaf pool handed out since the last cache rebuild
 };
 
 struct Partial {
@@ -152,6 +154,11 @@ struct View {
     // and the element's node positions when they were collected.
     uint32_t *cache_leaf;
     uint8_t *cache_n;
+    // Leaf lists of elements with more than kCacheLeaves leaves: a bump
+    // pool (reset at each cache rebuild); such an element's first two
+    // cache_leaf slots hold its offset and count.
+    uint32_t *leaf_pool;
+    uint32_t leaf_pool_capacity;
     float *cache_x32;  // FP32 node positions when the leaves were collected [E][6]
     // Mixed contact pass in three launches: FP32 vertex records of every
     // triangle in leaf order (a, b, c as three float4, the triangle index in
@@ -184,6 +191,20 @@ struct View {
     double young, poisson, shear_corr;
     int has_collider;
 };
+
+// Next free slot of a work list whose length is *count, for every lane that
+// calls it: the lanes that arrive together take consecutive slots with one
+// atomic (a per-lane atomic on one address serialises at L2 when tens of
+// thousands of elements append in one launch).  Slot order within a list is
+// not meaningful to any of its consumers.
+__device__ __forceinline__ uint32_t append_slot(uint32_t *count)
+{
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, g.size());
+    return g.shfl(base, 0) + g.thread_rank();
+}
 
 __device__ __forceinline__ V load3(const double *p) { return dm::v(p[0], p[1], p[2]); }
 __device__ __forceinline__ void store3(double *p, V a) { p[0] = a.x; p[1] = a.y; p[2] = a.z; }
@@ -337,10 +358,11 @@ template<class F> __device__ void bvh_query_packed(const View &d, V lo, V hi, do
 constexpr int kCacheLeaves = 32;
 constexpr double kCacheSlack = 1.0e-3;  // metres each node may move before the cache is bypassed
 constexpr uint8_t kCacheInvalid = 0xff;
+constexpr uint8_t kCacheBig = 0xfe;     // cache_n of an element whose leaves live in the leaf pool
 
 // Leaves whose FP32 outward box overlaps (lo, hi) padded by pad, in DFS
-// order, written to out (at most cap); returns the count, or cap + 1 on
-// overflow.
+// order; the first cap are written to out, and the return value is the
+// count of all of them.
 __device__ uint32_t collect_leaves(const View &d, V lo, V hi, double pad, uint32_t *out, uint32_t cap)
 {
     const QueryBox q = make_query(lo, hi, pad);
@@ -350,11 +372,23 @@ __device__ uint32_t collect_leaves(const View &d, V lo, V hi, double pad, uint32
         const uint32_t escape = __float_as_uint(a.w), leaf = __float_as_uint(b.w);
         if (!maybe_overlap(q, a, b)) { i = escape; continue; }
         if (leaf == 0) { ++i; continue; }
-        if (n == cap) return cap + 1;
-        out[n++] = i;
+        if (n < cap) out[n] = i;
+        ++n;
         i = escape;
     }
     return n;
+}
+
+// The cached leaf list of element e with cache state nl (its cache_n):
+// the element's own slots, or its range of the leaf pool; nullptr without
+// a cache.
+__device__ __forceinline__ const uint32_t *cached_leaves(const View &d, uint32_t e, uint8_t nl, uint32_t &count)
+{
+    const uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
+    if (nl == kCacheInvalid) { count = 0; return nullptr; }
+    if (nl == kCacheBig) { count = slots[1]; return d.leaf_pool + slots[0]; }
+    count = nl;
+    return slots;
 }
 
 // Candidates of leaves given as a list (the cached leaves), with the exact
@@ -966,9 +1000,24 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
                 // short leaf list (an element that left its slack would
                 // otherwise walk the tree twice in every evaluation).
                 const V s3 = dm::v(kCacheSlack, kCacheSlack, kCacheSlack);
+                const V clo = dm::vmin(xi, xj) - s3, chi = dm::vmax(xi, xj) + s3;
                 uint32_t *slots = d.cache_leaf + size_t(kCacheLeaves) * e;
-                const uint32_t c = collect_leaves(d, dm::vmin(xi, xj) - s3, dm::vmax(xi, xj) + s3, pad, slots, kCacheLeaves);
-                nl = c <= uint32_t(kCacheLeaves) ? uint8_t(c) : kCacheInvalid;
+                const uint32_t c = collect_leaves(d, clo, chi, pad, slots, kCacheLeaves);
+                if (c <= uint32_t(kCacheLeaves)) {
+                    nl = uint8_t(c);
+                } else {
+                    // A dense patch of the collider (a mesh pole, a seam):
+                    // the list goes to the pool, and k_contact_near works
+                    // through it 32 leaves at a time.
+                    const uint32_t off = atomicAdd(&d.sc->pool_used, c);
+                    nl = kCacheInvalid;
+                    if (size_t(off) + c <= d.leaf_pool_capacity) {
+                        collect_leaves(d, clo, chi, pad, d.leaf_pool + off, c);
+                        slots[0] = off;
+                        slots[1] = c;
+                        nl = kCacheBig;
+                    }
+                }
                 d.cache_n[e] = nl;
                 c32[0] = xi32.x; c32[1] = xi32.y; c32[2] = xi32.z; c32[3] = xj32.x; c32[4] = xj32.y; c32[5] = xj32.z;
                 inside = nl != kCacheInvalid;
@@ -976,7 +1025,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
             if (inside) {
                 if (nl > 0) {
                     // k_contact_near finishes the element, one warp over its leaves.
-                    d.near_list[atomicAdd(&d.sc->near_count, 1u)] = e;
+                    d.near_list[append_slot(&d.sc->near_count)] = e;
                     deferred = true;
                 }
             } else {
@@ -1028,6 +1077,116 @@ __global__ void __launch_bounds__(kBlock) k_contact_filter(View d, const double 
 // triangle order within the leaf, as in the single-lane filter; survivors
 // are compacted in that order (a prefix over lanes, then ascending within a
 // lane), so slots, the FP64 pass and the ordered selection are unchanged.
+// Triangle range (first, cnt) of cached leaf k of a list of `count` when
+// its box passes the query's exact per-leaf test; cnt = 0 otherwise.
+__device__ __forceinline__ void near_leaf(const View &d, const uint32_t *leaves, uint32_t k, uint32_t count, const QueryBox &qb,
+                                          uint32_t &first, uint32_t &cnt)
+{
+    first = 0;
+    cnt = 0;
+    if (k >= count) return;
+    const uint32_t node = leaves[k];
+    const float4 a = __ldg(d.bnode + 2 * size_t(node)), b = __ldg(d.bnode + 2 * size_t(node) + 1);
+    if (maybe_overlap(qb, a, b) && leaf_overlap_exact(d, node, a, b, qb)) {
+        const uint32_t leaf = __float_as_uint(b.w);
+        first = leaf >> 4;
+        cnt = leaf & 15u;
+    }
+}
+
+__device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t v, int lane)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+
+// Result of one element of the warp-cooperative contact pass (lane 0
+// writes): candidate count, survivor count or overflow, the no-contact
+// record, and the survivors' entries in the FP64 work list.
+__device__ __forceinline__ void near_finish(const View &d, uint32_t e, uint32_t total, uint32_t n, int lane)
+{
+    uint32_t base = 0;
+    if (lane == 0) {
+        d.c_cand[e] = total;
+        if (n > uint32_t(kSurvivors)) {
+            d.surv_n[e] = kSurvOverflow;
+        } else {
+            d.surv_n[e] = uint8_t(n);
+            if (n == 0) {
+                dm::ClosestPair pair;
+                pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
+                write_contact(d, e, kNone, pair);
+            } else {
+                base = atomicAdd(&d.sc->surv_count, n);
+            }
+        }
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (n <= uint32_t(kSurvivors) && uint32_t(lane) < n) d.surv_list[base + lane] = uint32_t(kSurvivors) * e + lane;
+}
+
+// An element whose cached leaves live in the leaf pool (more than 32): the
+// list is taken 32 leaves at a time, once for the FP32 bound and once more
+// for the survivors, which are written in leaf order.  Kept out of line so
+// the common one-round path keeps its registers.
+__device__ __noinline__ void near_pool_element(const View &d, uint32_t e, const QueryBox &qb, dm::F3 origin, dm::F3 p1)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const dm::F3 p0 = dm::f3(0.f, 0.f, 0.f);
+    uint32_t nleaves = 0;
+    const uint32_t *leaves = cached_leaves(d, e, kCacheBig, nleaves);
+    uint32_t total = 0;
+    float ub = 3.0e38f;
+    for (uint32_t r0 = 0; r0 < nleaves; r0 += 32) {
+        uint32_t first, cnt;
+        near_leaf(d, leaves, r0 + lane, nleaves, qb, first, cnt);
+        for (uint32_t r = 0; r < cnt; ++r) {
+            float m;
+            uint32_t t;
+            const float df = record_distance_f(d, first + r, origin, p0, p1, m, t);
+            ub = fminf(ub, df + m);
+        }
+        total += __shfl_sync(FULL, warp_inclusive_sum(cnt, lane), 31);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ub = fminf(ub, __shfl_xor_sync(FULL, ub, o));
+    uint32_t *slots = d.surv_tri + size_t(kSurvivors) * e;
+    uint32_t n = 0;
+    for (uint32_t r0 = 0; r0 < nleaves; r0 += 32) {
+        uint32_t first, cnt;
+        near_leaf(d, leaves, r0 + lane, nleaves, qb, first, cnt);
+        uint32_t mine = 0;
+        for (uint32_t r = 0; r < cnt; ++r) {
+            float m;
+            uint32_t t;
+            const float df = record_distance_f(d, first + r, origin, p0, p1, m, t);
+            mine += !(df - m > ub) ? 1u : 0u;
+        }
+        const uint32_t sincl = warp_inclusive_sum(mine, lane);
+        uint32_t slot = n + sincl - mine;
+        for (uint32_t r = 0; r < cnt && mine; ++r) {
+            float m;
+            uint32_t t;
+            const float df = record_distance_f(d, first + r, origin, p0, p1, m, t);
+            if (df - m > ub) continue;
+            if (slot < uint32_t(kSurvivors)) slots[slot] = t;
+            ++slot;
+        }
+        n += __shfl_sync(FULL, sincl, 31);
+    }
+    near_finish(d, e, total, n, lane);
+}
+
+// One warp per element queued by k_contact_filter (leaves cached and the
+// element within its slack): lane l tests cached leaf l and the FP32
+// distances of its triangles; the smallest upper bound is reduced across
+// the warp and the survivors are written in traversal order (leaf, then
+// triangle), so the first-found tie-break is kept.
 __global__ void __launch_bounds__(kBlock) k_contact_near(View d)
 {
     const unsigned FULL = 0xffffffffu;
@@ -1044,26 +1203,16 @@ __global__ void __launch_bounds__(kBlock) k_contact_near(View d)
         const float lo32[3] = {fminf(xi32.x, xj32.x), fminf(xi32.y, xj32.y), fminf(xi32.z, xj32.z)};
         const float hi32[3] = {fmaxf(xi32.x, xj32.x), fmaxf(xi32.y, xj32.y), fmaxf(xi32.z, xj32.z)};
         const QueryBox qb = make_query_f(lo32, hi32, dm::vmin(xi, xj), dm::vmax(xi, xj), pad);
-        const uint32_t nl = d.cache_n[e];
-        uint32_t first = 0, cnt = 0;
-        if (uint32_t(lane) < nl) {
-            const uint32_t node = d.cache_leaf[size_t(kCacheLeaves) * e + lane];
-            const float4 a = __ldg(d.bnode + 2 * size_t(node)), b = __ldg(d.bnode + 2 * size_t(node) + 1);
-            if (maybe_overlap(qb, a, b) && leaf_overlap_exact(d, node, a, b, qb)) {
-                const uint32_t leaf = __float_as_uint(b.w);
-                first = leaf >> 4;
-                cnt = leaf & 15u;
-            }
-        }
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
         const dm::F3 origin = xi32, p0 = dm::f3(0.f, 0.f, 0.f);
         const dm::F3 p1 = dm::f3(xj32.x - origin.x, xj32.y - origin.y, xj32.z - origin.z);
+        const uint8_t nl = d.cache_n[e];
+        if (nl == kCacheBig) {
+            near_pool_element(d, e, qb, origin, p1);
+            continue;
+        }
+        uint32_t first, cnt;
+        near_leaf(d, d.cache_leaf + size_t(kCacheLeaves) * e, lane, nl, qb, first, cnt);
+        const uint32_t total = __shfl_sync(FULL, warp_inclusive_sum(cnt, lane), 31);
         float lb[kLeafTriangles];
         uint32_t tri[kLeafTriangles];
         float ub = 3.0e38f;
@@ -1083,12 +1232,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_near(View d)
         uint32_t mine = 0;
 #pragma unroll
         for (int r = 0; r < kLeafTriangles; ++r) mine += (uint32_t(r) < cnt && !(lb[r] > ub)) ? 1u : 0u;
-        uint32_t sincl = mine;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(FULL, sincl, o);
-            if (lane >= o) sincl += v;
-        }
+        const uint32_t sincl = warp_inclusive_sum(mine, lane);
         const uint32_t n = __shfl_sync(FULL, sincl, 31);
         uint32_t slot = sincl - mine;
         uint32_t *slots = d.surv_tri + size_t(kSurvivors) * e;
@@ -1099,24 +1243,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_near(View d)
                 ++slot;
             }
         }
-        uint32_t base = 0;
-        if (lane == 0) {
-            d.c_cand[e] = total;
-            if (n > uint32_t(kSurvivors)) {
-                d.surv_n[e] = kSurvOverflow;
-            } else {
-                d.surv_n[e] = uint8_t(n);
-                if (n == 0) {
-                    dm::ClosestPair pair;
-                    pair.distance = 1.0e300; pair.t = 0.0; pair.bary = dm::v(1, 0, 0);
-                    write_contact(d, e, kNone, pair);
-                } else {
-                    base = atomicAdd(&d.sc->surv_count, n);
-                }
-            }
-        }
-        base = __shfl_sync(FULL, base, 0);
-        if (n <= uint32_t(kSurvivors) && uint32_t(lane) < n) d.surv_list[base + lane] = uint32_t(kSurvivors) * e + lane;
+        near_finish(d, e, total, n, lane);
     }
 }
 
@@ -1153,12 +1280,13 @@ __global__ void __launch_bounds__(kBlock) k_contact_select(View d, const double 
         const dm::F3 xi32 = dm::f3(d.q32[3 * size_t(i)], d.q32[3 * size_t(i) + 1], d.q32[3 * size_t(i) + 2]);
         const dm::F3 xj32 = dm::f3(d.q32[3 * size_t(j)], d.q32[3 * size_t(j) + 1], d.q32[3 * size_t(j) + 2]);
         const bool inside = nl != kCacheInvalid && within_cache_slack(d.cache_x32 + 6 * size_t(e), xi32, xj32);
-        const uint32_t *leaves = d.cache_leaf + size_t(kCacheLeaves) * e;
+        uint32_t nleaves = 0;
+        const uint32_t *leaves = cached_leaves(d, e, nl, nleaves);
         const V lo = dm::vmin(xi, xj), hi = dm::vmax(xi, xj);
         uint32_t c2 = 0;
         dm::ClosestPair pair;
         const uint32_t closest =
-            inside ? closest_triangle_in(d, xi, xj, c2, pair, [&](auto &&fn) { leaves_query(d, leaves, nl, lo, hi, pad, fn); })
+            inside ? closest_triangle_in(d, xi, xj, c2, pair, [&](auto &&fn) { leaves_query(d, leaves, nleaves, lo, hi, pad, fn); })
                    : closest_triangle<true>(d, xi, xj, pad, c2, pair);
         write_contact(d, e, closest, pair);
         return;
@@ -2185,7 +2313,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_collect(View d)
         uint32_t t;
         const float df = record_distance_f(d, p, origin, f0, f1, m, t);
         if (__fmul_rd(0.8f, __fsub_rd(__fsub_rd(df, m), target_ru)) >= speed_ru) return;
-        const uint32_t slot = atomicAdd(&d.sc->pair_count, 1u);
+        const uint32_t slot = append_slot(&d.sc->pair_count);
         if (slot < d.pair_capacity) { d.pair_elem[slot] = e; d.pair_tri[slot] = t; }
     };
     const uint8_t nl = d.cache_n[e];
@@ -2198,7 +2326,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_collect(View d)
     }
     if (cached) {
         // k_ccd_near tests the cached leaves, one warp per element.
-        if (nl > 0) d.near_list[atomicAdd(&d.sc->ccd_near, 1u)] = e;
+        if (nl > 0) d.near_list[append_slot(&d.sc->ccd_near)] = e;
     } else {
         bvh_positions_packed(d, qb, test);
     }
@@ -2216,8 +2344,9 @@ __global__ void __launch_bounds__(kBlock) k_ccd_near(View d)
     const float target_ru = __double2float_ru(target);
     for (uint32_t k = warp; k < count; k += nwarps) {
         const uint32_t e = d.near_list[k];
-        const uint32_t nl = d.cache_n[e];
-        if (uint32_t(lane) >= nl) continue;
+        uint32_t nleaves = 0;
+        const uint32_t *leaves = cached_leaves(d, e, d.cache_n[e], nleaves);
+        if (uint32_t(lane) >= nleaves) continue;
         const uint32_t i = d.ei[e], j = d.ej[e];
         const V p0 = load3(d.q + 6 * size_t(i)), p1 = load3(d.q + 6 * size_t(j));
         const V d0 = load3(d.dir + 6 * size_t(i)), d1 = load3(d.dir + 6 * size_t(j));
@@ -2230,17 +2359,20 @@ __global__ void __launch_bounds__(kBlock) k_ccd_near(View d)
         const dm::F3 f1 = dm::f3(d.q32[3 * size_t(j)] - origin.x, d.q32[3 * size_t(j) + 1] - origin.y,
                                  d.q32[3 * size_t(j) + 2] - origin.z);
         const float speed_ru = __fmul_ru(__double2float_ru(speed), 1.000002f);
-        const uint32_t node = d.cache_leaf[size_t(kCacheLeaves) * e + lane];
-        const float4 a = __ldg(d.bnode + 2 * size_t(node)), b = __ldg(d.bnode + 2 * size_t(node) + 1);
-        if (!maybe_overlap(qb, a, b) || !leaf_overlap_exact(d, node, a, b, qb)) continue;
-        const uint32_t leaf = __float_as_uint(b.w), first = leaf >> 4, cnt = leaf & 15u;
-        for (uint32_t p = first; p < first + cnt; ++p) {
-            float m;
-            uint32_t t;
-            const float df = record_distance_f(d, p, origin, f0, f1, m, t);
-            if (__fmul_rd(0.8f, __fsub_rd(__fsub_rd(df, m), target_ru)) >= speed_ru) continue;
-            const uint32_t slot = atomicAdd(&d.sc->pair_count, 1u);
-            if (slot < d.pair_capacity) { d.pair_elem[slot] = e; d.pair_tri[slot] = t; }
+        // Lane l takes leaves l, l + 32, ... of the cached list.
+        for (uint32_t c = lane; c < nleaves; c += 32) {
+            const uint32_t node = leaves[c];
+            const float4 a = __ldg(d.bnode + 2 * size_t(node)), b = __ldg(d.bnode + 2 * size_t(node) + 1);
+            if (!maybe_overlap(qb, a, b) || !leaf_overlap_exact(d, node, a, b, qb)) continue;
+            const uint32_t leaf = __float_as_uint(b.w), first = leaf >> 4, cnt = leaf & 15u;
+            for (uint32_t p = first; p < first + cnt; ++p) {
+                float m;
+                uint32_t t;
+                const float df = record_distance_f(d, p, origin, f0, f1, m, t);
+                if (__fmul_rd(0.8f, __fsub_rd(__fsub_rd(df, m), target_ru)) >= speed_ru) continue;
+                const uint32_t slot = append_slot(&d.sc->pair_count);
+                if (slot < d.pair_capacity) { d.pair_elem[slot] = e; d.pair_tri[slot] = t; }
+            }
         }
     }
 }
@@ -2356,6 +2488,7 @@ __global__ void k_init_scalars(View d)
     d.sc->refine_bits = 0;
     d.sc->near_count = 0;
     d.sc->ccd_near = 0;
+    d.sc->pool_used = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -2625,6 +2758,8 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     const size_t pair_capacity = std::min<size_t>(std::max<size_t>(size_t(1) << 20, 8 * E), size_t(16) << 20);
     bytes += 2 * padded<double>(E) + padded<double>(3 * E) + 2 * padded<uint32_t>(pair_capacity);
     bytes += padded<uint32_t>(size_t(kCacheLeaves) * E) + padded<uint8_t>(E);
+    const size_t leaf_pool = std::min<size_t>(std::max<size_t>(size_t(1) << 20, 4 * E), size_t(16) << 20);
+    bytes += padded<uint32_t>(leaf_pool);
     bytes += padded<float>(3 * N) + padded<float>(6 * E);
     bytes += padded<uint32_t>(E);
     bytes += 2 * padded<float2>(36 * N) + padded<float2>(6 * N) + padded<float>(N);
@@ -2678,6 +2813,7 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     v.pair_elem = a.take<uint32_t>(pair_capacity); v.pair_tri = a.take<uint32_t>(pair_capacity);
     v.pair_capacity = uint32_t(pair_capacity);
     v.cache_leaf = a.take<uint32_t>(size_t(kCacheLeaves) * E); v.cache_n = a.take<uint8_t>(E);
+    v.leaf_pool = a.take<uint32_t>(leaf_pool); v.leaf_pool_capacity = uint32_t(leaf_pool);
     v.cache_x32 = a.take<float>(6 * E);
     v.tri32 = a.take<float4>(3 * T); v.tri32_old = a.take<float4>(3 * T);
     v.ff_inv = a.take<float2>(36 * N); v.ff_c = a.take<float2>(36 * N); v.ff_d = a.take<float2>(6 * N);
@@ -3003,6 +3139,7 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
              trial ? 1 : 0, trial ? alpha : 0.0, dt);
     if (mode_ && v.has_collider) {
         const double *q = v.q;
+        if (rebuild_cache_) KHS_CUDA(cudaMemsetAsync(&v.sc->pool_used, 0, sizeof(uint32_t), I.stream));
         I.launch(rebuild_cache_ ? "k_contact_filter_rebuild" : trial ? "k_contact_filter_trial" : "k_contact_filter", k_contact_filter,
                  grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
         I.launch("k_contact_near", k_contact_near, 152 * 8, kBlock, v);

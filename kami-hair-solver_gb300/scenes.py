@@ -240,6 +240,49 @@ def sphere_scene(seed: int = 1, strands: int = 64, nodes: int = 32, length: floa
                  collider_at, seed)
 
 
+def pole_scene(seed: int = 4, strands: int = 48, nodes: int = 32, seg: float = 1.0e-3, frames: int = 2,
+               substeps: int = 4, segments: int = 360, rings: int = 120) -> Scene:
+    """Strands lying across the pole of a UV sphere (0.1 m, ``segments``
+    x ``rings``), where ``segments`` sliver triangles meet in one vertex: a
+    dense patch of the collider, so that elements near the pole reach
+    hundreds of leaves.  Roots on a ring 2-6 mm from the pole, strands tilted
+    70 degrees from the normal towards the pole axis, 1 mm segments.  The
+    sphere turns about z (through the pole) and drifts."""
+    rng = np.random.default_rng(seed)
+    R = 0.1
+    v, f = uv_ellipsoid((0.0, 0.0, 0.0), (R, R, R), segments, rings)
+    strand_list = []
+    for k in range(strands):
+        rho = rng.uniform(0.002, 0.006)
+        ph = 2 * np.pi * k / strands + rng.uniform(0, 0.1)
+        n = np.array([rho * np.cos(ph), rho * np.sin(ph), math.sqrt(R * R - rho * rho)]) / R
+        inward = -np.array([np.cos(ph), np.sin(ph), 0.0])
+        inward -= n * np.dot(inward, n)
+        inward /= np.linalg.norm(inward)
+        tilt = math.radians(70.0 + rng.uniform(-5.0, 5.0))
+        d = math.cos(tilt) * n + math.sin(tilt) * inward
+        root = n * (R + 1.0e-4)
+        strand_list.append(root[None, :] + np.arange(nodes)[:, None] * seg * d[None, :])
+    points, offsets = _assemble(strand_list)
+    fps = 24.0
+
+    def transform(frame: int):
+        t = frame / fps
+        return _rotation_z(1.5 * t), np.array([0.004, -0.002, 0.0]) * t
+
+    def roots_at(frame: int) -> np.ndarray:
+        Rm, tr = transform(frame)
+        return points @ Rm.T + tr
+
+    def collider_at(frame: int) -> np.ndarray:
+        Rm, tr = transform(frame)
+        return v @ Rm.T + tr
+
+    desc = dict(substeps=substeps, maximum_substeps=max(32, substeps), fixed_root_nodes=2)
+    return Scene("pole", points, offsets, v, f, frames + 1, fps, desc, dict(HAIR_MATERIAL_SMALL), roots_at,
+                 collider_at, seed)
+
+
 def ellipsoid_scene(seed: int = 2, strands: int = 1000, node_range=(20, 120), frames: int = 10, substeps: int = 8,
                     level: int = 5, angular_velocity: float = 2.0, axes=(0.09, 0.11, 0.12)) -> Scene:
     """Helical strands (curl radius U[2,10] mm, pitch U[5,20] mm, 2 mm +-10 %

@@ -119,6 +119,24 @@ def test_mixed_ellipsoid_contact(gpu_lib, oracle_lib):
     _check(rep, rot_tol)
 
 
+def test_mixed_pole_dense_leaves(gpu_lib, oracle_lib):
+    """Elements next to the pole of a UV sphere, where 360 sliver triangles
+    meet, reach hundreds of BVH leaves: more than the 32 an element caches,
+    so the mixed form keeps their leaf lists in the leaf pool and the
+    warp-cooperative passes take them 32 at a time.  The mixed form must
+    reproduce the plain form's trajectory bit for bit, and at its own state
+    the oracle's per-element contact classification."""
+    mixed = parity.run(gpu_lib, scenes.pole_scene(frames=2), mode=kn.MODE_MIXED, probe=oracle_lib)
+    plain = parity.run(gpu_lib, scenes.pole_scene(frames=2), mode=kn.MODE_PLAIN_FP64)
+    assert max(int(fr["contacts"]["candidate_count"].max()) for fr in mixed) > 32 * 8
+    assert len(mixed) == len(plain) == 2
+    for k, (fm, fp) in enumerate(zip(mixed, plain)):
+        assert fm["result"] == fp["result"] == kn.OK, (k, fm["error"], fp["error"])
+        assert np.array_equal(fm["q"], fp["q"]) and np.array_equal(fm["v"], fp["v"]), k
+        assert all(v == 0 for v in parity.records_equal(fm["contacts"], fp["contacts"]).values()), k
+        assert all(v == 0 for v in parity.records_equal(fm["contacts"], fm["probe_contacts"]).values()), k
+
+
 def test_mixed_contact_query_bitexact(gpu_lib, oracle_lib):
     """The FP32 broadphase + FP32-filtered narrow phase classifies every
     element exactly like the FP64 oracle (candidate counts, closest
