@@ -430,6 +430,27 @@ KHS_API KhsResult khsxSetRollbackRing(KhsSolver *solver, uint32_t slots);
    call steps frame + 1. */
 KHS_API KhsResult khsxRollbackToFrame(KhsSolver *solver, uint32_t frame);
 
+/* Output ring for baking (replaces the reference add-on's per-frame
+   synchronous khsCopyOriginalPositions, addon.py:748-757; the per-frame
+   checkpoint it also takes is covered by khsxSetRollbackRing).  After each
+   successful khsStepAnimationFrame (frame 0 included) the original points'
+   positions are gathered on the device and copied to pinned host memory on
+   a second stream, overlapping the next frame; the last `slots` frames are
+   kept (24 bytes per point per slot, on the device and pinned on the host).
+   slots 0 frees the ring.  Requires a built solver. */
+KHS_API KhsResult khsxSetOutputRing(KhsSolver *solver, uint32_t slots);
+
+/* Waits for `frame`'s copy and writes its positions (capacity >= the
+   original point count).  KHS_ERROR_INVALID_STATE with the ring off,
+   KHS_ERROR_INVALID_ARGUMENT if the ring does not hold the frame. */
+KHS_API KhsResult khsxCopyOutputFrame(KhsSolver *solver, uint32_t frame, KhsVec3 *positions,
+                                      uint32_t capacity);
+
+/* As khsxCopyOutputFrame, but returns a pointer to the pinned slot itself
+   (no host copy), valid until `slots` more frames are stepped or the ring
+   is changed. */
+KHS_API KhsResult khsxMapOutputFrame(KhsSolver *solver, uint32_t frame, const KhsVec3 **positions);
+
 /* Copies the full generalised state: q and v are 6 * internal_node_count
    FP64 values each, per-node interleaved (x, y, z, rx, ry, rz).  Either
    pointer may be NULL. */

@@ -630,6 +630,33 @@ KHS_API KhsResult khsxRollbackToFrame(KhsSolver *s, uint32_t frame)
     });
 }
 
+KHS_API KhsResult khsxSetOutputRing(KhsSolver *s, uint32_t slots)
+{
+    return guarded(s, [&] {
+        if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+        return s->from_engine(s->engine->set_output_ring(slots));
+    });
+}
+
+KHS_API KhsResult khsxCopyOutputFrame(KhsSolver *s, uint32_t frame, KhsVec3 *positions, uint32_t capacity)
+{
+    return guarded(s, [&] {
+        if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+        if (!positions) return KHS_ERROR_INVALID_ARGUMENT;
+        return s->from_engine(s->engine->output_frame(frame, positions, capacity, nullptr));
+    });
+}
+
+KHS_API KhsResult khsxMapOutputFrame(KhsSolver *s, uint32_t frame, const KhsVec3 **positions)
+{
+    return guarded(s, [&] {
+        if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+        if (!positions) return KHS_ERROR_INVALID_ARGUMENT;
+        *positions = nullptr;
+        return s->from_engine(s->engine->output_frame(frame, nullptr, 0, positions));
+    });
+}
+
 KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *s, uint32_t strands_per_warp, uint32_t blocks_per_sm,
                                             uint32_t long_strands)
 {

@@ -2647,6 +2647,31 @@ struct Engine::Impl {
     // slot k holding frame ring_frame[k] (-1 = empty), [slots][2][N][6] FP64.
     double *ring = nullptr;
     std::vector<int64_t> ring_frame;
+    // Output ring: the original points' positions of the last
+    // out_frame.size() animation frames, gathered on the solver's stream after
+    // each frame and copied to pinned host memory on copy_stream, so the copy
+    // overlaps the next frame ([slots][P][3] FP64 on both sides).
+    cudaStream_t copy_stream = nullptr;
+    double *out_dev = nullptr, *out_host = nullptr;
+    std::vector<cudaEvent_t> out_gathered, out_copied;
+    std::vector<int64_t> out_frame;
+    size_t out_bytes = 0;
+    uint32_t out_next = 0;
+    void release_output()
+    {
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
+        for (cudaEvent_t e : out_gathered) cudaEventDestroy(e);
+        for (cudaEvent_t e : out_copied) cudaEventDestroy(e);
+        out_gathered.clear();
+        out_copied.clear();
+        if (out_dev) cudaFree(out_dev);
+        if (out_host) cudaFreeHost(out_host);
+        out_dev = out_host = nullptr;
+        resident -= out_bytes;
+        out_bytes = 0;
+        out_frame.clear();
+        out_next = 0;
+    }
     void (*solve_kernel)(View) = nullptr;
     uint32_t solve_long = 0;  // > 0: k_block_solve_hybrid with this many long strands
     std::vector<uint32_t> sorted_len;  // free nodes per strand, in the solve order
@@ -2707,6 +2732,8 @@ struct Engine::Impl {
         if (ring) cudaFree(ring);
         if (anim_root_x) cudaFree(anim_root_x);
         if (root_work) cudaFree(root_work);
+        release_output();
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (mail_host) cudaFreeHost(mail_host);
         if (sweep_host) cudaFreeHost(sweep_host);
         if (ev_begin) cudaEventDestroy(ev_begin);
@@ -3580,7 +3607,11 @@ KhsResult Engine::step_animation_frame(uint32_t frame, double frame_dt)
 {
     Impl &I = *d_;
     if (!animation_ready_ || frame >= animation_frames_) return fail(KHS_ERROR_INVALID_ARGUMENT, "invalid animation frame index");
-    if (frame == 0) { current_frame_ = 0; return KHS_OK; }
+    if (frame == 0) {
+        current_frame_ = 0;
+        push_output(0);
+        return KHS_OK;
+    }
     if (frame != current_frame_ + 1) return fail(KHS_ERROR_INVALID_STATE, "animation frames must be stepped in order");
     const size_t N3 = 3 * size_t(I.v.N), V3 = 3 * size_t(I.v.V);
     const uint32_t a = frame - 1, b = frame;
@@ -3590,8 +3621,74 @@ KhsResult Engine::step_animation_frame(uint32_t frame, double frame_dt)
     if (r == KHS_OK) {
         current_frame_ = frame;
         push_ring(frame);
+        push_output(frame);
     }
     return r;
+}
+
+void Engine::push_output(uint32_t frame)
+{
+    Impl &I = *d_;
+    if (!I.out_dev || !I.original_count) return;
+    const uint32_t k = I.out_next;
+    I.out_next = uint32_t((k + 1) % I.out_frame.size());
+    const size_t per = 3 * size_t(I.original_count);
+    double *dst = I.out_dev + k * per;
+    // The slot's previous copy must have finished before the gather
+    // overwrites it; an event never recorded does not wait.
+    KHS_CUDA(cudaStreamWaitEvent(I.stream, I.out_copied[k], 0));
+    I.launch("k_gather", k_gather, grid_for(I.original_count), kBlock, I.v.q, I.mapping_dev, I.original_count, dst);
+    KHS_CUDA(cudaEventRecord(I.out_gathered[k], I.stream));
+    KHS_CUDA(cudaStreamWaitEvent(I.copy_stream, I.out_gathered[k], 0));
+    KHS_CUDA(cudaMemcpyAsync(I.out_host + k * per, dst, per * 8, cudaMemcpyDeviceToHost, I.copy_stream));
+    KHS_CUDA(cudaEventRecord(I.out_copied[k], I.copy_stream));
+    I.out_frame[k] = int64_t(frame);
+}
+
+KhsResult Engine::set_output_ring(uint32_t slots)
+{
+    Impl &I = *d_;
+    if (slots > 1024) return fail(KHS_ERROR_INVALID_ARGUMENT, "output ring holds at most 1024 frames");
+    I.sync();
+    I.release_output();
+    if (!slots) return KHS_OK;
+    const size_t bytes = size_t(slots) * 3 * size_t(I.original_count) * 8;
+    if (!I.copy_stream) KHS_CUDA(cudaStreamCreateWithFlags(&I.copy_stream, cudaStreamNonBlocking));
+    if (cudaMalloc(reinterpret_cast<void **>(&I.out_dev), std::max<size_t>(bytes, 256)) != cudaSuccess ||
+        cudaHostAlloc(reinterpret_cast<void **>(&I.out_host), std::max<size_t>(bytes, 256), cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        if (I.out_dev) cudaFree(I.out_dev);
+        I.out_dev = I.out_host = nullptr;
+        return fail(KHS_ERROR_OUT_OF_MEMORY, "cannot allocate the output ring");
+    }
+    I.out_bytes = bytes;
+    I.resident += bytes;
+    gpu_stats_.resident_bytes = I.resident;
+    I.out_gathered.resize(slots);
+    I.out_copied.resize(slots);
+    for (uint32_t k = 0; k < slots; ++k) {
+        KHS_CUDA(cudaEventCreateWithFlags(&I.out_gathered[k], cudaEventDisableTiming));
+        KHS_CUDA(cudaEventCreateWithFlags(&I.out_copied[k], cudaEventDisableTiming));
+    }
+    I.out_frame.assign(slots, -1);
+    I.out_next = 0;
+    return KHS_OK;
+}
+
+KhsResult Engine::output_frame(uint32_t frame, KhsVec3 *out, uint32_t capacity, const KhsVec3 **view)
+{
+    Impl &I = *d_;
+    if (!I.out_dev) return fail(KHS_ERROR_INVALID_STATE, "the output ring is off");
+    size_t k = I.out_frame.size();
+    for (size_t s = 0; s < I.out_frame.size(); ++s)
+        if (I.out_frame[s] == int64_t(frame)) k = s;
+    if (k == I.out_frame.size()) return fail(KHS_ERROR_INVALID_ARGUMENT, "the frame is not in the output ring");
+    if (out && capacity < I.original_count) return fail(KHS_ERROR_INVALID_ARGUMENT, "output buffer smaller than the point count");
+    KHS_CUDA(cudaEventSynchronize(I.out_copied[k]));
+    const double *src = I.out_host + k * 3 * size_t(I.original_count);
+    if (view) *view = reinterpret_cast<const KhsVec3 *>(src);
+    if (out) std::memcpy(out, src, size_t(I.original_count) * 24);
+    return KHS_OK;
 }
 
 void Engine::push_ring(uint32_t frame)

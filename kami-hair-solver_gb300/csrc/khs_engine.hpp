@@ -66,6 +66,13 @@ public:
     // (q and v), filled after every successful animation frame.
     KhsResult set_rollback_ring(uint32_t slots);
     KhsResult rollback_to_frame(uint32_t frame);
+    // Pinned output ring of the last `slots` animation frames' original-point
+    // positions, copied from the device on a second stream after every frame
+    // (0 turns it off).  output_frame waits for the frame's copy, then copies
+    // it to `out` (capacity >= the point count) and/or returns a view of the
+    // pinned slot, valid until `slots` more frames are stepped.
+    KhsResult set_output_ring(uint32_t slots);
+    KhsResult output_frame(uint32_t frame, KhsVec3 *out, uint32_t capacity, const KhsVec3 **view);
 
     KhsResult copy_original_positions(KhsVec3 *out, uint32_t capacity) const;
     KhsResult copy_internal_positions(KhsVec3 *out, uint32_t capacity) const;
@@ -106,6 +113,7 @@ private:
 
     KhsResult fail(KhsResult r, const std::string &message);
     KhsResult run_root_pass(const KhsVec3 *points, uint32_t count);
+    void push_output(uint32_t frame);
     void clear_failure();
     void set_failure_context(uint32_t kind, uint32_t frame, uint32_t sub, uint32_t attempted, uint32_t maximum,
                              uint32_t attempts);

@@ -210,6 +210,9 @@ EXTENSION_FUNCTIONS = [
     ("khsxRollbackToFrame", ctypes.c_int, [VP, c_u32]),
     ("khsxQueryContactsNoAlloc", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
     ("khsxComputeRootTargets", ctypes.c_int, [VP, VP, c_u32, VP, VP, c_u32]),
+    ("khsxSetOutputRing", ctypes.c_int, [VP, c_u32]),
+    ("khsxCopyOutputFrame", ctypes.c_int, [VP, c_u32, VP, c_u32]),
+    ("khsxMapOutputFrame", ctypes.c_int, [VP, c_u32, P(VP)]),
     ("khsxSetProfiling", ctypes.c_int, [VP, c_u32]),
     ("khsxGetKernelTimings", c_u32, [VP, VP, c_u32]),
     ("khsxResetKernelTimings", ctypes.c_int, [VP]),
@@ -220,7 +223,8 @@ EXTENSION_FUNCTIONS = [
 # Entry points the CPU oracle does not provide (device-only measurement).
 DEVICE_ONLY = {"khsxSetProfiling", "khsxGetKernelTimings", "khsxResetKernelTimings", "khsxGetKernelLaunchCount",
                "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc", "khsxSetBlockSolveSchedule",
-               "khsxSetRollbackRing", "khsxRollbackToFrame"}
+               "khsxSetRollbackRing", "khsxRollbackToFrame", "khsxSetOutputRing", "khsxCopyOutputFrame",
+               "khsxMapOutputFrame"}
 
 # Size of the file-scope device scratch behind khsxQueryContactsNoAlloc
 # (KHSX_NO_ALLOC_SCRATCH_BYTES in the C header).
@@ -499,6 +503,27 @@ class HairSolver:
         if out.dtype != CONTACT_DTYPE or not out.flags.c_contiguous:
             raise ValueError("out must be a contiguous CONTACT_DTYPE array")
         return int(self._library.khsxQueryContactsNoAlloc(self._handle, _ptr(q), q.size, _ptr(out), out.size))
+
+    def set_output_ring(self, slots: int):
+        self._check(self._library.khsxSetOutputRing(self._handle, int(slots)))
+
+    def output_frame(self, frame: int) -> np.ndarray:
+        """khsxCopyOutputFrame: (P, 3) positions of an animation frame."""
+        n = int(self._library.khsGetOriginalPointCount(self._handle))
+        out = np.zeros((n, 3), dtype=np.float64)
+        self._check(self._library.khsxCopyOutputFrame(self._handle, int(frame), _ptr(out), n))
+        return out
+
+    def map_output_frame(self, frame: int) -> np.ndarray:
+        """khsxMapOutputFrame: a read-only view of the pinned slot (valid
+        until the ring moves past the frame)."""
+        n = int(self._library.khsGetOriginalPointCount(self._handle))
+        ptr = ctypes.c_void_p()
+        self._check(self._library.khsxMapOutputFrame(self._handle, int(frame), ctypes.byref(ptr)))
+        buf = (ctypes.c_double * (3 * n)).from_address(ptr.value)
+        view = np.frombuffer(buf, dtype=np.float64).reshape(n, 3)
+        view.flags.writeable = False
+        return view
 
     def compute_root_targets(self, points) -> tuple[np.ndarray, np.ndarray]:
         """khsxComputeRootTargets: (positions, rotation vectors) of every
