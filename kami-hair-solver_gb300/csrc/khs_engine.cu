@@ -24,7 +24,8 @@
 //   evaluation    k_node_eval, [mixed: k_contact_filter, k_contact_near (warp
 //                 per element with cached leaves), k_contact_exact (thread per
 //                 FP32 survivor), k_contact_select], k_elem_eval, k_node_sum
-//                 (thread per block entry), k_reduce_eval, k_final_eval
+//                 (thread per block entry), k_reduce_eval (both levels: the
+//                 last block to finish reduces the partials)
 //   direction     k_block_solve_aug<H> / k_block_solve_hybrid (persistent
 //                 warps, strand groups from a longest-first queue),
 //                 [float-float form: k_ff_factor, k_ff_residual, k_ff_correct],
@@ -98,6 +99,7 @@ struct Scalars {
     uint32_t refine_bits; // largest relative refinement correction (FP32 bits)
     uint32_t near_count;  // elements queued for the warp-cooperative contact pass
     uint32_t ccd_near;    // elements queued for the warp-cooperative CCD pass
+    uint32_t eval_done;   // blocks of k_reduce_eval finished (the last one reduces the partials)
     uint32_t pool_used;   // entries of the leaf pool handed out since the last cache rebuild
 };
 
@@ -1465,54 +1467,43 @@ __global__ void __launch_bounds__(kBlock) k_node_sum(View d)
     }
 }
 
-// Block-level tree sum of one double per thread (blockDim == kBlock).
-__device__ double block_sum(double x, double *sh)
+// K block-level tree reductions (sums, minima or maxima, by Op) at once,
+// one value per thread each (blockDim == kBlock), in the order of the plain
+// shared-memory tree sh[t] = f(sh[t], sh[t + s]) for s = 128, 64, ..., 1:
+// levels 128, 64 and 32 in shared memory, then 16 ... 1 by shuffles in the
+// first warp (lane t combines lane t + s exactly as the tree would), with 4
+// barriers for all K values.  Every thread receives the results.
+struct OpSum { template<class T> __device__ static T f(T a, T b) { return a + b; } };
+struct OpMin { __device__ static double f(double a, double b) { return fmin(a, b); } };
+struct OpMax { __device__ static double f(double a, double b) { return fmax(a, b); } };
+
+template<class Op, int K, class T> __device__ void block_tree(T (&x)[K], T (*sh)[kBlock])
 {
-    sh[threadIdx.x] = x;
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][t] = x[k];
     __syncthreads();
-    for (int s = kBlock / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+#pragma unroll
+    for (int s = kBlock / 2; s >= 32; s >>= 1) {
+        if (t < s) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) sh[k][t] = Op::f(sh[k][t], sh[k][t + s]);
+        }
         __syncthreads();
     }
-    const double r = sh[0];
-    __syncthreads();
-    return r;
-}
-__device__ double block_min(double x, double *sh)
-{
-    sh[threadIdx.x] = x;
-    __syncthreads();
-    for (int s = kBlock / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
-        __syncthreads();
+    if (t < 32) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            T v = sh[k][t];
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) v = Op::f(v, __shfl_down_sync(0xffffffffu, v, s));
+            if (t == 0) sh[k][0] = v;
+        }
     }
-    const double r = sh[0];
     __syncthreads();
-    return r;
-}
-__device__ double block_max(double x, double *sh)
-{
-    sh[threadIdx.x] = x;
+#pragma unroll
+    for (int k = 0; k < K; ++k) x[k] = sh[k][0];
     __syncthreads();
-    for (int s = kBlock / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
-        __syncthreads();
-    }
-    const double r = sh[0];
-    __syncthreads();
-    return r;
-}
-__device__ unsigned long long block_sum_u(unsigned long long x, unsigned long long *sh)
-{
-    sh[threadIdx.x] = x;
-    __syncthreads();
-    for (int s = kBlock / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    const unsigned long long r = sh[0];
-    __syncthreads();
-    return r;
 }
 
 __device__ __forceinline__ void chunk(uint32_t count, uint32_t &begin, uint32_t &end)
@@ -1523,10 +1514,42 @@ __device__ __forceinline__ void chunk(uint32_t count, uint32_t &begin, uint32_t 
 }
 
 // First reduction level over nodes and elements of this block's chunk.
+// Final level of the evaluation sums over the per-block partials, in block
+// order, published to the host mailbox (run by the last block of
+// k_reduce_eval to finish).
+__device__ void final_eval(const View &d, double (*sh)[kBlock], unsigned long long (*shu)[kBlock])
+{
+    double v[6] = {0, 0, 0, 0, 0, 0};  // energy, kinetic, grad2, elastic, contact, and min gap below
+    v[5] = __longlong_as_double(0x7ff0000000000000LL);
+    unsigned long long u[3] = {0, 0, 0};
+    for (int b = threadIdx.x; b < kPartials; b += kBlock) {
+        const Partial *p = d.partials + b;
+        v[0] += __ldcg(&p->node_energy); v[1] += __ldcg(&p->kinetic); v[2] += __ldcg(&p->grad2);
+        v[3] += __ldcg(&p->elastic); v[4] += __ldcg(&p->contact);
+        v[5] = fmin(v[5], __ldcg(&p->min_gap));
+        u[0] += __ldcg(&p->candidates); u[1] += __ldcg(&p->active); u[2] += (unsigned long long)__ldcg(&p->infeasible);
+    }
+    double sums[5] = {v[0], v[1], v[2], v[3], v[4]}, mins[1] = {v[5]};
+    block_tree<OpSum>(sums, sh);
+    block_tree<OpMin>(mins, sh);
+    block_tree<OpSum>(u, shu);
+    if (threadIdx.x == 0) {
+        Mailbox *m = d.mail;
+        m->objective = (sums[0] + sums[3]) + sums[4];
+        m->elastic = sums[3]; m->contact = sums[4]; m->kinetic = sums[1]; m->minimum_gap = mins[0]; m->grad_norm2 = sums[2];
+        m->candidates = u[0]; m->active = u[1]; m->feasible = u[2] ? 0 : 1;
+    }
+}
+
+// Both reduction levels of an evaluation in one launch: each block sums its
+// chunk of nodes and elements into a partial; the last block to finish
+// (counted with an atomic after a fence) reduces the partials in block
+// order, so the result does not depend on which block that is.
 __global__ void __launch_bounds__(kBlock) k_reduce_eval(View d, int gradient)
 {
-    __shared__ double sh[kBlock];
-    __shared__ unsigned long long shu[kBlock];
+    __shared__ double sh[5][kBlock];
+    __shared__ unsigned long long shu[3][kBlock];
+    __shared__ bool last;
     uint32_t nb, ne, eb, ee;
     chunk(d.N, nb, ne);
     chunk(d.E, eb, ee);
@@ -1548,41 +1571,25 @@ __global__ void __launch_bounds__(kBlock) k_reduce_eval(View d, int gradient)
         if (f & kFlagActive) ++act;
         if (f & kFlagInfeasible) inf = 1;
     }
-    Partial p;
-    p.node_energy = block_sum(en, sh);
-    p.kinetic = block_sum(ki, sh);
-    p.grad2 = block_sum(g2, sh);
-    p.elastic = block_sum(el, sh);
-    p.contact = block_sum(co, sh);
-    p.min_gap = block_min(mg, sh);
-    p.candidates = block_sum_u(cand, shu);
-    p.active = block_sum_u(act, shu);
-    p.infeasible = int(block_sum_u((unsigned long long)inf, shu) != 0);
-    p.pad = 0;
-    if (threadIdx.x == 0) d.partials[blockIdx.x] = p;
-}
-
-__global__ void __launch_bounds__(kBlock) k_final_eval(View d)
-{
-    __shared__ double sh[kBlock];
-    __shared__ unsigned long long shu[kBlock];
-    double en = 0, ki = 0, g2 = 0, el = 0, co = 0, mg = __longlong_as_double(0x7ff0000000000000LL);
-    unsigned long long cand = 0, act = 0, inf = 0;
-    for (int b = threadIdx.x; b < kPartials; b += kBlock) {
-        const Partial p = d.partials[b];
-        en += p.node_energy; ki += p.kinetic; g2 += p.grad2; el += p.elastic; co += p.contact;
-        mg = fmin(mg, p.min_gap);
-        cand += p.candidates; act += p.active; inf += p.infeasible;
-    }
-    en = block_sum(en, sh); ki = block_sum(ki, sh); g2 = block_sum(g2, sh);
-    el = block_sum(el, sh); co = block_sum(co, sh); mg = block_min(mg, sh);
-    cand = block_sum_u(cand, shu); act = block_sum_u(act, shu); inf = block_sum_u(inf, shu);
+    double sums[5] = {en, ki, g2, el, co}, mins[1] = {mg};
+    unsigned long long u[3] = {cand, act, (unsigned long long)inf};
+    block_tree<OpSum>(sums, sh);
+    block_tree<OpMin>(mins, sh);
+    block_tree<OpSum>(u, shu);
     if (threadIdx.x == 0) {
-        Mailbox *m = d.mail;
-        m->objective = (en + el) + co;
-        m->elastic = el; m->contact = co; m->kinetic = ki; m->minimum_gap = mg; m->grad_norm2 = g2;
-        m->candidates = cand; m->active = act; m->feasible = inf ? 0 : 1;
+        Partial p;
+        p.node_energy = sums[0]; p.kinetic = sums[1]; p.grad2 = sums[2]; p.elastic = sums[3]; p.contact = sums[4];
+        p.min_gap = mins[0];
+        p.candidates = u[0]; p.active = u[1]; p.infeasible = int(u[2] != 0); p.pad = 0;
+        d.partials[blockIdx.x] = p;
+        __threadfence();
+        last = atomicAdd(&d.sc->eval_done, 1u) == gridDim.x - 1;
     }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    final_eval(d, sh, shu);
+    if (threadIdx.x == 0) d.sc->eval_done = 0;
 }
 
 // ---- direction ----------------------------------------------------------
@@ -2180,7 +2187,7 @@ __global__ void __launch_bounds__(kBlock) k_scale(View d, double s)
 // g.d, |d|^2 and the largest free-node translation of d.
 __global__ void __launch_bounds__(kBlock) k_reduce_dir(View d)
 {
-    __shared__ double sh[kBlock];
+    __shared__ double sh2[2][kBlock];
     uint32_t nb, ne;
     chunk(d.N, nb, ne);
     double gd = 0.0, dd = 0.0, mx = 0.0;
@@ -2192,22 +2199,30 @@ __global__ void __launch_bounds__(kBlock) k_reduce_dir(View d)
         }
         if (!d.fixed[n]) mx = fmax(mx, dm::norm(load3(d.dir + 6 * size_t(n))));
     }
-    DirPartial p;
-    p.slope = block_sum(gd, sh);
-    p.dnorm2 = block_sum(dd, sh);
-    p.max_translation = block_max(mx, sh);
-    if (threadIdx.x == 0) d.dpartials[blockIdx.x] = p;
+    double sums[2] = {gd, dd}, maxs[1] = {mx};
+    block_tree<OpSum>(sums, sh2);
+    block_tree<OpMax>(maxs, sh2);
+    if (threadIdx.x == 0) {
+        DirPartial p;
+        p.slope = sums[0];
+        p.dnorm2 = sums[1];
+        p.max_translation = maxs[0];
+        d.dpartials[blockIdx.x] = p;
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_final_dir(View d)
 {
-    __shared__ double sh[kBlock];
+    __shared__ double sh2[2][kBlock];
     double gd = 0, dd = 0, mx = 0;
     for (int b = threadIdx.x; b < kPartials; b += kBlock) {
         const DirPartial p = d.dpartials[b];
         gd += p.slope; dd += p.dnorm2; mx = fmax(mx, p.max_translation);
     }
-    gd = block_sum(gd, sh); dd = block_sum(dd, sh); mx = block_max(mx, sh);
+    double sums[2] = {gd, dd}, maxs[1] = {mx};
+    block_tree<OpSum>(sums, sh2);
+    block_tree<OpMax>(maxs, sh2);
+    gd = sums[0]; dd = sums[1]; mx = maxs[0];
     if (threadIdx.x == 0) {
         d.mail->slope = gd; d.mail->dir_norm2 = dd; d.mail->max_translation = mx;
         d.mail->ccd_bits = d.sc->ccd_bits;
@@ -2489,6 +2504,7 @@ __global__ void k_init_scalars(View d)
     d.sc->near_count = 0;
     d.sc->ccd_near = 0;
     d.sc->pool_used = 0;
+    d.sc->eval_done = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather(const double *q, const uint32_t *map, uint32_t count, double *out)
@@ -3178,7 +3194,6 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
              kBlock, v, gradient ? 1 : 0);
     if (gradient) I.launch("k_node_sum", k_node_sum, grid_for(42 * size_t(v.N)), kBlock, v);
     I.launch("k_reduce_eval", k_reduce_eval, kPartials, kBlock, v, gradient ? 1 : 0);
-    I.launch("k_final_eval", k_final_eval, 1, kBlock, v);
     I.check();
     I.sync();
     const Mailbox &mb = *I.mail_host;
