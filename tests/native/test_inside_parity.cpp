@@ -3,13 +3,17 @@
 // all-triangle loop (src/solver.cpp:608-632) as the oracle restates it
 // (ray_crosses_triangle, oracle/khs_oracle_math.hpp): the inside flag of
 // every point must be the same.  Usage:
-//   test_inside_parity vertices.bin triangles.bin points.bin
-// (FP64 [V][3], uint32 [T][3], FP64 [P][3]).  Built and run by
-// tests/test_inside_parity.py.
+//   test_inside_parity vertices.bin triangles.bin points.bin [sample]
+// (FP64 [V][3], uint32 [T][3], FP64 [P][3]).  With `sample`, the BVH walk
+// is timed over every point and the all-triangle loop over every sample-th
+// point only (its time is scaled to all points); the flags of the sampled
+// points are compared.  Built and run by tests/test_inside_parity.py.
 #include "khs_model.hpp"
 #include "khs_oracle_math.hpp"
 
+#include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <vector>
 
@@ -25,10 +29,11 @@ template<class T> static std::vector<T> read_all(const char *path)
 
 int main(int argc, char **argv)
 {
-    if (argc != 4) {
-        std::printf("usage: %s vertices.bin triangles.bin points.bin\n", argv[0]);
+    if (argc != 4 && argc != 5) {
+        std::printf("usage: %s vertices.bin triangles.bin points.bin [sample]\n", argv[0]);
         return 2;
     }
+    const size_t sample = argc == 5 ? size_t(std::atol(argv[4])) : 1;
     const std::vector<double> verts = read_all<double>(argv[1]), pts = read_all<double>(argv[3]);
     const std::vector<uint32_t> tris = read_all<uint32_t>(argv[2]);
     khs::Model m;
@@ -39,11 +44,15 @@ int main(int argc, char **argv)
     for (size_t k = 0; k < points.size(); ++k) points[k] = {pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]};
 
     std::vector<uint8_t> fast;
+    const auto t0 = std::chrono::steady_clock::now();
     khs::inside_closed_collider(m, points, fast);
+    const auto t1 = std::chrono::steady_clock::now();
 
     using khs_oracle::v3;
     long mismatches = 0, inside = 0;
-    for (size_t k = 0; k < points.size(); ++k) {
+    size_t checked = 0;
+    for (size_t k = 0; k < points.size(); k += sample) {
+        ++checked;
         const khs_oracle::V3 p = v3(points[k].x, points[k].y, points[k].z);
         uint32_t hits = 0;
         for (size_t t = 0; t < tris.size() / 3; ++t) {
@@ -57,8 +66,13 @@ int main(int argc, char **argv)
             ++mismatches;
         }
     }
-    std::printf("inside parity: %zu points (%ld inside), %zu triangles, %ld mismatches\n", points.size(), inside,
+    const auto t2 = std::chrono::steady_clock::now();
+    const double bvh_s = std::chrono::duration<double>(t1 - t0).count();
+    const double loop_s = std::chrono::duration<double>(t2 - t1).count() * double(points.size()) / double(checked);
+    std::printf("inside parity: %zu points checked (%ld inside), %zu triangles, %ld mismatches\n", checked, inside,
                 tris.size() / 3, mismatches);
+    std::printf("time for all %zu points: BVH walk %.3f s, all-triangle loop %.1f s%s\n", points.size(), bvh_s, loop_s,
+                sample > 1 ? " (scaled from the sample)" : "");
     std::printf(mismatches == 0 ? "PASS\n" : "FAIL\n");
     return mismatches == 0 ? 0 : 1;
 }

@@ -69,3 +69,25 @@ def test_bvh_inside_test_matches_all_triangle_loop(tmp_path):
         assert out.returncode == 0 and "PASS" in out.stdout, name + ": " + out.stdout + out.stderr
         inside = int(out.stdout.split("(")[1].split()[0])
         assert 0 < inside < len(pts), (name, inside)
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_bvh_inside_test_on_a_large_request(tmp_path):
+    """The hair points of the largest serving request (20,000 strands,
+    1.77M points) against its 20,480-triangle closed ellipsoid: the BVH walk
+    over all points, checked against the all-triangle loop on every 500th
+    point, whose time is scaled to all points (printed)."""
+    exe = tmp_path / "inside_parity"
+    csrc = REPO / "kami-hair-solver_gb300" / "csrc"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{csrc}", f"-I{REPO / 'oracle'}",
+                    f"-I{REPO / 'include'}", str(REPO / "tests" / "native" / "test_inside_parity.cpp"),
+                    str(csrc / "khs_model.cpp"), "-o", str(exe)], check=True)
+    sc = scenes.ellipsoid_scene(seed=7, strands=20000, node_range=(16, 160), frames=1, level=5,
+                                axes=(0.095, 0.11, 0.12))
+    files = [tmp_path / f"{k}.bin" for k in ("v", "t", "p")]
+    np.ascontiguousarray(sc.vertices, dtype=np.float64).tofile(files[0])
+    np.ascontiguousarray(sc.triangles, dtype=np.uint32).tofile(files[1])
+    np.ascontiguousarray(sc.points, dtype=np.float64).tofile(files[2])
+    out = subprocess.run([str(exe), *map(str, files), "500"], capture_output=True, text=True)
+    print(out.stdout)
+    assert out.returncode == 0 and "PASS" in out.stdout, out.stdout + out.stderr
