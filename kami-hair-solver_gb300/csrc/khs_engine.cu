@@ -3647,6 +3647,8 @@ void Engine::push_output(uint32_t frame)
     if (!I.out_dev || !I.original_count) return;
     const uint32_t k = I.out_next;
     I.out_next = uint32_t((k + 1) % I.out_frame.size());
+    for (int64_t &held : I.out_frame)
+        if (held == int64_t(frame)) held = -1;  // an older pass over this frame (before a rollback)
     const size_t per = 3 * size_t(I.original_count);
     double *dst = I.out_dev + k * per;
     // The slot's previous copy must have finished before the gather
@@ -3658,6 +3660,14 @@ void Engine::push_output(uint32_t frame)
     KHS_CUDA(cudaMemcpyAsync(I.out_host + k * per, dst, per * 8, cudaMemcpyDeviceToHost, I.copy_stream));
     KHS_CUDA(cudaEventRecord(I.out_copied[k], I.copy_stream));
     I.out_frame[k] = int64_t(frame);
+}
+
+// Outputs of frames after `frame` belong to a trajectory that a rollback or
+// a checkpoint restore has left.
+void Engine::drop_outputs_after(uint32_t frame)
+{
+    for (int64_t &held : d_->out_frame)
+        if (held > int64_t(frame)) held = -1;
 }
 
 KhsResult Engine::set_output_ring(uint32_t slots)
@@ -3756,6 +3766,7 @@ KhsResult Engine::rollback_to_frame(uint32_t frame)
     // Frames after the restored one are no longer on this trajectory.
     for (size_t j = 0; j < slots; ++j)
         if (I.ring_frame[j] > int64_t(frame)) I.ring_frame[j] = -1;
+    drop_outputs_after(frame);
     current_frame_ = frame;
     cancel_.store(false);
     progress_frame_.store(frame);
@@ -3819,6 +3830,7 @@ KhsResult Engine::restore_checkpoint(const void *data, uint64_t size)
     KHS_CUDA(cudaMemcpyAsync(I.v_snap, I.v.v, qb, cudaMemcpyDeviceToDevice, I.stream));
     I.sync();
     current_frame_ = h.animation_frame;
+    drop_outputs_after(h.animation_frame);
     cancel_.store(false);
     progress_frame_.store(h.animation_frame);
     progress_substep_.store(0); progress_substep_count_.store(0); progress_iteration_.store(0);

@@ -114,6 +114,7 @@ private:
     KhsResult fail(KhsResult r, const std::string &message);
     KhsResult run_root_pass(const KhsVec3 *points, uint32_t count);
     void push_output(uint32_t frame);
+    void drop_outputs_after(uint32_t frame);
     void clear_failure();
     void set_failure_context(uint32_t kind, uint32_t frame, uint32_t sub, uint32_t attempted, uint32_t maximum,
                              uint32_t attempts);

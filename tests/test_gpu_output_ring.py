@@ -6,7 +6,8 @@ after every frame, addon.py:748-757).
 * Every frame the ring holds equals khsCopyOriginalPositions right after
   that frame, bit for bit, through both the copy and the mapped view.
 * Frames the ring has moved past, and frames not stepped yet, are refused;
-  so are reads with the ring off.
+  so are reads with the ring off, and frames past the one a rollback
+  restored.
 * The ring does not change the solve: the final state is the same bits
   with and without it.
 * Timing on the body scene: the per-frame output through the ring against
@@ -69,6 +70,29 @@ def test_output_ring_matches_synchronous_copy(gpu_lib):
         assert np.array_equal(plain.state()[0], q_ring)
     finally:
         plain.close()
+
+
+def test_output_ring_after_rollback(gpu_lib):
+    """After khsxRollbackToFrame the ring drops the frames past the restored
+    one (they belong to the abandoned trajectory) and holds each re-stepped
+    frame once, equal to the positions after it."""
+    sc = scenes.sphere_scene(motion=True, frames=6)
+    s = _frames(gpu_lib, sc, 4, 6)
+    try:
+        s.set_rollback_ring(6)
+        for f in range(0, 5):
+            s.step_animation_frame(f, sc.frame_dt)
+        s._check(s._library.khsxRollbackToFrame(s.handle, 2))
+        out = np.zeros((int(s._library.khsGetOriginalPointCount(s.handle)), 3))
+        for gone in (3, 4):
+            assert s._library.khsxCopyOutputFrame(s.handle, gone, ctypes.c_void_p(out.ctypes.data), len(out)) == \
+                kn.ERROR_INVALID_ARGUMENT, gone
+        assert s.output_frame(2) is not None
+        for f in (3, 4):
+            s.step_animation_frame(f, sc.frame_dt)
+            assert np.array_equal(s.output_frame(f), s.positions()), f
+    finally:
+        s.close()
 
 
 def test_output_ring_timing_body_scene(gpu_lib):
