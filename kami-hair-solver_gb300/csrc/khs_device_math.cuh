@@ -86,11 +86,11 @@ KHS_HD void rotation_and_jacobian(V u, const double *ref, M &R, M *Jl)
 {
     const double t2 = dot(u, u);
     double a, b;
-    double s, c;
+    double s;
     if (t2 < 1.0e-10) {
         a = 1.0 - t2 / 6.0 + t2 * t2 / 120.0;
         b = 0.5 - t2 / 24.0 + t2 * t2 / 720.0;
-        s = 0.0; c = 1.0;
+        s = 0.0;
     } else {
         // Half-angle form: one sincos, and 1 - cos t = 2 sin^2(t/2) without
         // cancellation (it is also the left Jacobian's coefficient p).
@@ -98,7 +98,6 @@ KHS_HD void rotation_and_jacobian(V u, const double *ref, M &R, M *Jl)
         double sh, ch;
         sincos(0.5 * t, &sh, &ch);
         s = 2.0 * sh * ch;
-        c = 1.0 - 2.0 * sh * sh;
         a = s * it;
         b = 2.0 * sh * sh * (it * it);
     }

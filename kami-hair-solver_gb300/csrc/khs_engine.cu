@@ -1594,37 +1594,6 @@ __global__ void __launch_bounds__(kBlock) k_reduce_eval(View d, int gradient)
 
 // ---- direction ----------------------------------------------------------
 
-// Gauss-Jordan 6x6 inverse with partial pivoting after a relative diagonal
-// shift (cuda_backend.cu:855-864).
-__device__ bool inverse6(double a[36], double inv[36])
-{
-    for (int k = 0; k < 36; ++k) inv[k] = 0.0;
-    for (int k = 0; k < 6; ++k) inv[7 * k] = 1.0;
-    double scale = 0.0;
-    for (int k = 0; k < 6; ++k) scale = fmax(scale, fabs(a[7 * k]));
-    for (int k = 0; k < 6; ++k) a[7 * k] += fmax(1.0e-12 * scale, 1.0e-24);
-    for (int col = 0; col < 6; ++col) {
-        int pivot = col;
-        double best = fabs(a[6 * col + col]);
-        for (int row = col + 1; row < 6; ++row)
-            if (fabs(a[6 * row + col]) > best) { best = fabs(a[6 * row + col]); pivot = row; }
-        if (best < 1.0e-30 || !isfinite(best)) return false;
-        if (pivot != col)
-            for (int k = 0; k < 6; ++k) {
-                double t = a[6 * col + k]; a[6 * col + k] = a[6 * pivot + k]; a[6 * pivot + k] = t;
-                t = inv[6 * col + k]; inv[6 * col + k] = inv[6 * pivot + k]; inv[6 * pivot + k] = t;
-            }
-        const double ip = 1.0 / a[6 * col + col];
-        for (int k = 0; k < 6; ++k) { a[6 * col + k] *= ip; inv[6 * col + k] *= ip; }
-        for (int row = 0; row < 6; ++row)
-            if (row != col) {
-                const double f = a[6 * row + col];
-                for (int k = 0; k < 6; ++k) { a[6 * row + k] -= f * a[6 * col + k]; inv[6 * row + k] -= f * inv[6 * col + k]; }
-            }
-    }
-    return true;
-}
-
 // Block-tridiagonal Thomas solve per strand (cuda_backend.cu:866-881) with
 // the reference's Gauss-Jordan elimination, partial pivoting on the first
 // largest |pivot|, after the relative diagonal shift max(1e-12 max|a_ii|,

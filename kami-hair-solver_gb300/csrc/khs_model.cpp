@@ -1,5 +1,6 @@
 // Host-side rod model builder (see khs_model.hpp).
 #include "khs_model.hpp"
+#include "khs_device_math.cuh"
 
 #include <algorithm>
 #include <limits>
@@ -43,14 +44,6 @@ inline Mat from_columns(Vec a, Vec b, Vec c)
     r.m[6] = a.z; r.m[7] = b.z; r.m[8] = c.z;
     return r;
 }
-inline Mat times_transpose(const Mat &a, const Mat &b)  // a * b^T
-{
-    Mat r;
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j)
-            r.m[3 * i + j] = (a.m[3 * i] * b.m[3 * j] + a.m[3 * i + 1] * b.m[3 * j + 1]) + a.m[3 * i + 2] * b.m[3 * j + 2];
-    return r;
-}
 inline Mat transpose_times(const Mat &a, const Mat &b)  // a^T * b
 {
     Mat r;
@@ -69,88 +62,32 @@ Vec cayley(const Mat &q)
     return mk(s * v.x, s * v.y, s * v.z);
 }
 
-// Frame with the tangent as third column, first column from the hint
-// (math.hpp:26-43).
-Mat tangent_frame(Vec tangent, Vec hint)
+// Root and reference frames (math.hpp:26-58, solver.cpp:19-26) use the
+// same functions as the device root-target kernels (khs_device_math.cuh,
+// compiled here for the host), so the two round identically.
+inline dm::V to_dm(Vec a) { return dm::v(a.x, a.y, a.z); }
+inline Vec from_dm(dm::V a) { return mk(a.x, a.y, a.z); }
+inline dm::M to_dm(const Mat &a)
 {
-    const Vec d3 = unit(tangent);
-    Vec d1 = sub(hint, mul(d3, dot(hint, d3)));
-    if (sq(d1) < 1.0e-16) {
-        const Vec axis = std::fabs(d3.x) < 0.8 ? mk(1, 0, 0) : mk(0, 1, 0);
-        d1 = sub(axis, mul(d3, dot(axis, d3)));
-    }
-    d1 = unit(d1);
-    const Vec d2 = unit(cross(d3, d1));
-    d1 = unit(cross(d2, d3));
-    return from_columns(d1, d2, d3);
+    dm::M r;
+    for (int k = 0; k < 9; ++k) r.m[k] = a.m[k];
+    return r;
+}
+inline Mat from_dm(const dm::M &a)
+{
+    Mat r;
+    for (int k = 0; k < 9; ++k) r.m[k] = a.m[k];
+    return r;
 }
 
-// Any unit vector orthogonal to s, chosen like Eigen's unitOrthogonal.
-Vec orthogonal_unit(Vec s)
-{
-    const double eps = 1e-12;
-    if (!(std::fabs(s.x) <= std::fabs(s.z) * eps) || !(std::fabs(s.y) <= std::fabs(s.z) * eps)) {
-        const double inv = 1.0 / std::sqrt(s.x * s.x + s.y * s.y);
-        return mk(-s.y * inv, s.x * inv, 0.0);
-    }
-    const double inv = 1.0 / std::sqrt(s.y * s.y + s.z * s.z);
-    return mk(0.0, -s.z * inv, s.y * inv);
-}
+// Frame with the tangent as third column, first column from the hint.
+Mat tangent_frame(Vec tangent, Vec hint) { return from_dm(dm::frame_from_tangent(to_dm(tangent), to_dm(hint))); }
 
-// Minimal rotation of a director between consecutive tangents
-// (math.hpp:45-58).
-Vec transport(Vec director, Vec from, Vec to)
-{
-    const Vec a = unit(from), b = unit(to);
-    const Vec axis = cross(a, b);
-    const double s = len(axis);
-    const double c = std::clamp(dot(a, b), -1.0, 1.0);
-    if (s < 1.0e-12) {
-        if (c > 0.0) return director;
-        const Vec n = orthogonal_unit(a);
-        return sub(mul(mul(n, 2.0), dot(n, director)), director);
-    }
-    const Vec n = divs(axis, s);
-    return add(add(mul(director, c), mul(cross(n, director), s)), mul(mul(n, dot(n, director)), 1.0 - c));
-}
+// Minimal rotation of a director between consecutive tangents.
+Vec transport(Vec director, Vec from, Vec to) { return from_dm(dm::parallel_transport(to_dm(director), to_dm(from), to_dm(to))); }
 
-// Rotation vector of a rotation matrix.  Shepperd's method (J. Guidance and
-// Control 1(3), 1978) gives the quaternion from the largest of its four
-// squared components; the angle is 2 atan2(|v|, |w|) and the axis v/|v|
-// carries the sign of w (the reference goes through Eigen::AngleAxisd,
-// solver.cpp:19-26).
-Vec rotation_vector(const Mat &r)
-{
-    double q[4];  // x y z w
-    const double tr = (r.m[0] + r.m[4]) + r.m[8];
-    if (tr > 0.0) {
-        double s = std::sqrt(tr + 1.0);
-        q[3] = 0.5 * s;
-        s = 0.5 / s;
-        q[0] = (r.m[7] - r.m[5]) * s;
-        q[1] = (r.m[2] - r.m[6]) * s;
-        q[2] = (r.m[3] - r.m[1]) * s;
-    } else {
-        int i = 0;
-        if (r.m[4] > r.m[0]) i = 1;
-        if (r.m[8] > r.m[4 * i]) i = 2;
-        const int j = (i + 1) % 3, k = (j + 1) % 3;
-        double s = std::sqrt(r.m[4 * i] - r.m[4 * j] - r.m[4 * k] + 1.0);
-        q[i] = 0.5 * s;
-        s = 0.5 / s;
-        q[3] = (r.m[3 * k + j] - r.m[3 * j + k]) * s;
-        q[j] = (r.m[3 * j + i] + r.m[3 * i + j]) * s;
-        q[k] = (r.m[3 * k + i] + r.m[3 * i + k]) * s;
-    }
-    double n = std::sqrt((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]);
-    if (!(n != 0.0)) return Vec{};
-    double angle = 2.0 * std::atan2(n, std::fabs(q[3]));
-    if (q[3] < 0.0) n = -n;
-    const Vec axis = mk(q[0] / n, q[1] / n, q[2] / n);
-    if (!std::isfinite(angle) || !finite(axis)) return Vec{};
-    if (angle > kPiHost) angle -= 2.0 * kPiHost;
-    return mul(axis, angle);
-}
+// Rotation vector of a rotation matrix.
+Vec rotation_vector(const Mat &r) { return from_dm(dm::rotation_vector(to_dm(r))); }
 
 // Unit central-difference tangents along one strand (solver.cpp:324-331).
 bool strand_tangents(const std::vector<Vec> &x, uint32_t first, uint32_t count, std::vector<Vec> &t, bool reject_zero)
@@ -536,10 +473,10 @@ bool root_targets(const Model &m, const std::vector<Vec> &points, std::vector<Ve
         const uint32_t first = m.strand_first[s], count = m.strand_count[s];
         if (!strand_tangents(pos, first, count, tangents, true)) return false;
         Mat f = tangent_frame(tangents[0], column(m.frame[first], 0));
-        rot[first] = rotation_vector(times_transpose(f, m.frame[first]));
+        rot[first] = rotation_vector(from_dm(dm::times_transpose(to_dm(f), to_dm(m.frame[first]))));
         for (uint32_t k = 1; k < count; ++k) {
             f = tangent_frame(tangents[k], transport(column(f, 0), tangents[k - 1], tangents[k]));
-            rot[first + k] = rotation_vector(times_transpose(f, m.frame[first + k]));
+            rot[first + k] = rotation_vector(from_dm(dm::times_transpose(to_dm(f), to_dm(m.frame[first + k]))));
         }
     }
     return true;

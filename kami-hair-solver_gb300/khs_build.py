@@ -66,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         jobs.append((cmd, BUILD / (unit + ".log"), obj))
     for unit in HOST_UNITS:
         obj = BUILD / (unit + ".o")
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall", "-Wextra",
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall", "-Wextra", "-Wno-unknown-pragmas",
                *common_inc, f"-I{os.environ.get('CUDA_HOME', '/usr/local/cuda')}/include", "-c", str(CSRC / unit),
                "-o", str(obj)]
         jobs.append((cmd, BUILD / (unit + ".log"), obj))
