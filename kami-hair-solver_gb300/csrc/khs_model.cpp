@@ -3,15 +3,45 @@
 #include "khs_device_math.cuh"
 
 #include <algorithm>
+#include <exception>
 #include <limits>
 #include <numeric>
 #include <sstream>
+#include <thread>
 #include <unordered_map>
 
 namespace khs {
 namespace {
 
 constexpr double kPiHost = 3.14159265358979323846;
+
+// Host threads for the build-time passes (the machine's cores, at most 32).
+inline unsigned host_threads()
+{
+    const unsigned n = std::thread::hardware_concurrency();
+    return std::max(1u, std::min(n ? n : 1u, 32u));
+}
+
+// f(begin, end, chunk) over contiguous chunks of [0, count), one per host
+// thread (the caller runs the first); exceptions reach the caller.
+template<class F> void parallel_chunks(size_t count, unsigned chunks, F &&f)
+{
+    chunks = unsigned(std::max<size_t>(1, std::min<size_t>(chunks, count)));
+    std::vector<std::exception_ptr> errors(chunks);
+    auto run = [&](unsigned c) {
+        try {
+            f(count * c / chunks, count * (c + 1) / chunks, c);
+        } catch (...) {
+            errors[c] = std::current_exception();
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned c = 1; c < chunks; ++c) pool.emplace_back(run, c);
+    run(0);
+    for (std::thread &t : pool) t.join();
+    for (const std::exception_ptr &e : errors)
+        if (e) std::rethrow_exception(e);
+}
 
 inline Vec mk(double x, double y, double z) { Vec v; v.x = x; v.y = y; v.z = z; return v; }
 inline Vec add(Vec a, Vec b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
@@ -127,8 +157,15 @@ struct TreeBuilder {
         const Vec s = add(add(vert(t, 0), vert(t, 1)), vert(t, 2));
         return device_flavour ? comp(s, axis) * (1.0 / 3.0) : comp(s, axis) / 3.0;
     }
-    int build(uint32_t begin, uint32_t end)
+    // Builds [begin, end) of `order` into `out` (root first, then the left
+    // subtree, then the right one) and returns the root's index there.  Up to
+    // `spawn` levels down, the right half is built on another thread into a
+    // vector of its own and appended after the left one, which gives the same
+    // nodes in the same order as the one-thread build: the two halves touch
+    // disjoint ranges of `order`.
+    int build(std::vector<TreeNode> &out, uint32_t begin, uint32_t end, int spawn)
     {
+        std::vector<TreeNode> &nodes = out;
         const int idx = int(nodes.size());
         nodes.push_back({});
         const double big = device_flavour ? 1e300 : std::numeric_limits<double>::infinity();
@@ -153,8 +190,29 @@ struct TreeBuilder {
         const uint32_t mid = begin + (end - begin) / 2;
         std::nth_element(order.begin() + begin, order.begin() + mid, order.begin() + end,
                          [&](uint32_t l, uint32_t r) { return centroid(l, axis) < centroid(r, axis); });
-        const int left = build(begin, mid);
-        const int right = build(mid, end);
+        int left, right;
+        if (spawn > 0 && end - begin >= 16384) {
+            std::vector<TreeNode> right_nodes;
+            std::exception_ptr error;
+            std::thread worker([&] {
+                try {
+                    build(right_nodes, mid, end, spawn - 1);
+                } catch (...) {
+                    error = std::current_exception();
+                }
+            });
+            left = build(nodes, begin, mid, spawn - 1);
+            worker.join();
+            if (error) std::rethrow_exception(error);
+            right = int(nodes.size());
+            for (TreeNode n : right_nodes) {
+                if (n.left >= 0) { n.left += right; n.right += right; }
+                nodes.push_back(n);
+            }
+        } else {
+            left = build(nodes, begin, mid, 0);
+            right = build(nodes, mid, end, 0);
+        }
         nodes[idx].left = left; nodes[idx].right = right; nodes[idx].count = 0;
         return idx;
     }
@@ -163,7 +221,9 @@ struct TreeBuilder {
         order.resize(tri.size() / 3);
         std::iota(order.begin(), order.end(), 0u);
         nodes.clear();
-        if (!order.empty()) build(0, uint32_t(order.size()));
+        int spawn = 0;
+        while ((2u << spawn) <= host_threads()) ++spawn;
+        if (!order.empty()) build(nodes, 0, uint32_t(order.size()), spawn);
     }
 };
 
@@ -513,28 +573,43 @@ double minimum_gap_host(const Model &m, const KhsHairMaterial &material, uint64_
 {
     TreeBuilder tb{m.collider, m.tri, false, {}, {}};
     tb.run();
-    double best = std::numeric_limits<double>::infinity();
-    uint64_t count = 0;
     const double pad = material.radius + material.collider_offset + material.barrier_distance;
-    std::vector<int> stack;
-    for (size_t e = 0; e < m.elements(); ++e) {
-        const uint32_t i = m.elem_i[e], j = m.elem_j[e];
-        if (m.fixed[i] || !m.elem_contact[e] || tb.nodes.empty()) continue;
-        const Vec lo = vmin(m.x[i], m.x[j]), hi = vmax(m.x[i], m.x[j]);
-        stack.assign(1, 0);
-        while (!stack.empty()) {
-            const TreeNode &nd = tb.nodes[stack.back()];
-            stack.pop_back();
-            if (!boxes_touch(lo, hi, nd.lo, nd.hi, pad)) continue;
-            if (nd.left >= 0) { stack.push_back(nd.left); stack.push_back(nd.right); continue; }
-            for (uint32_t k = nd.begin; k < nd.begin + nd.count; ++k) {
-                const uint32_t t = tb.order[k];
-                const double d = segment_triangle_distance(m.x[i], m.x[j], m.collider[m.tri[3 * t]],
-                                                           m.collider[m.tri[3 * t + 1]], m.collider[m.tri[3 * t + 2]]);
-                best = std::min(best, d - material.radius - material.collider_offset);
-                ++count;
+    // Elements in chunks on the host threads: the minimum and the count do
+    // not depend on the order the elements are visited in.
+    const unsigned chunks = host_threads();
+    std::vector<double> chunk_best(chunks, std::numeric_limits<double>::infinity());
+    std::vector<uint64_t> chunk_count(chunks, 0);
+    parallel_chunks(m.elements(), chunks, [&](size_t begin, size_t end, unsigned c) {
+        double best = std::numeric_limits<double>::infinity();
+        uint64_t count = 0;
+        std::vector<int> stack;
+        for (size_t e = begin; e < end; ++e) {
+            const uint32_t i = m.elem_i[e], j = m.elem_j[e];
+            if (m.fixed[i] || !m.elem_contact[e] || tb.nodes.empty()) continue;
+            const Vec lo = vmin(m.x[i], m.x[j]), hi = vmax(m.x[i], m.x[j]);
+            stack.assign(1, 0);
+            while (!stack.empty()) {
+                const TreeNode &nd = tb.nodes[stack.back()];
+                stack.pop_back();
+                if (!boxes_touch(lo, hi, nd.lo, nd.hi, pad)) continue;
+                if (nd.left >= 0) { stack.push_back(nd.left); stack.push_back(nd.right); continue; }
+                for (uint32_t k = nd.begin; k < nd.begin + nd.count; ++k) {
+                    const uint32_t t = tb.order[k];
+                    const double d = segment_triangle_distance(m.x[i], m.x[j], m.collider[m.tri[3 * t]],
+                                                               m.collider[m.tri[3 * t + 1]], m.collider[m.tri[3 * t + 2]]);
+                    best = std::min(best, d - material.radius - material.collider_offset);
+                    ++count;
+                }
             }
         }
+        chunk_best[c] = best;
+        chunk_count[c] = count;
+    });
+    double best = std::numeric_limits<double>::infinity();
+    uint64_t count = 0;
+    for (unsigned c = 0; c < chunks; ++c) {
+        best = std::min(best, chunk_best[c]);
+        count += chunk_count[c];
     }
     if (candidates) *candidates = count;
     return best;
@@ -545,15 +620,23 @@ bool initial_feasibility(const Model &m, const KhsSolverDesc &desc, const KhsHai
 {
     if (m.closed_manifold) {
         const InsideTester tester(m, m.x);
-        std::vector<int> stack;
-        for (size_t k = 0; k < m.nodes(); ++k) {
-            if (m.fixed[k] || m.virtual_extension[k]) continue;
-            if (tester.inside(m.x[k], stack)) {
-                std::ostringstream ss;
-                ss << "initial intersection: internal node " << k << " lies inside the closed collider";
-                error = ss.str();
-                return false;
+        // Nodes in chunks on the host threads; the error names the lowest
+        // inside node, as the one-thread scan would.
+        const unsigned chunks = host_threads();
+        std::vector<size_t> first_inside(chunks, m.nodes());
+        parallel_chunks(m.nodes(), chunks, [&](size_t begin, size_t end, unsigned c) {
+            std::vector<int> stack;
+            for (size_t k = begin; k < end; ++k) {
+                if (m.fixed[k] || m.virtual_extension[k]) continue;
+                if (tester.inside(m.x[k], stack)) { first_inside[c] = k; return; }
             }
+        });
+        const size_t k = *std::min_element(first_inside.begin(), first_inside.end());
+        if (k < m.nodes()) {
+            std::ostringstream ss;
+            ss << "initial intersection: internal node " << k << " lies inside the closed collider";
+            error = ss.str();
+            return false;
         }
     }
     uint64_t candidates = 0;
@@ -572,8 +655,10 @@ void inside_closed_collider(const Model &m, const std::vector<Vec> &points, std:
 {
     inside.assign(points.size(), 0);
     const InsideTester tester(m, points);
-    std::vector<int> stack;
-    for (size_t k = 0; k < points.size(); ++k) inside[k] = tester.inside(points[k], stack) ? 1 : 0;
+    parallel_chunks(points.size(), host_threads(), [&](size_t begin, size_t end, unsigned) {
+        std::vector<int> stack;
+        for (size_t k = begin; k < end; ++k) inside[k] = tester.inside(points[k], stack) ? 1 : 0;
+    });
 }
 
 void build_device_bvh(Model &m)
