@@ -467,12 +467,19 @@ typedef struct KhsxSubstepRecord {
     uint32_t steepest_fallbacks;
     uint32_t refinement_sweeps;    /* KHSX_MODE_MIXED_FF: FP64 refinement sweeps */
     uint32_t fp64_fallbacks;       /* KHSX_MODE_MIXED_FF: directions re-solved in FP64 */
-    uint32_t reserved;
+    uint32_t trust_scalings;       /* directions scaled down to the translation trust radius */
     uint64_t contact_candidates;
     uint64_t active_contacts;
     double final_residual_norm;
     double minimum_gap;
 } KhsxSubstepRecord;
+
+/* Ends every following frame after its first `substeps` substeps (0, the
+   default, runs whole frames).  A frame cut short returns KHS_OK with the
+   state after those substeps.  For sampled comparisons and timing of
+   partial frames against another implementation from one checkpoint; a
+   bake never sets it.  May be called before or after khsBuild. */
+KHS_API KhsResult khsxSetSubstepLimit(KhsSolver *solver, uint32_t substeps);
 
 /* Number of substep records of the last frame (last adaptive attempt). */
 KHS_API uint32_t khsxGetSubstepRecordCount(const KhsSolver *solver);

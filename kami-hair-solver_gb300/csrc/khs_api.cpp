@@ -54,6 +54,7 @@ struct KhsSolver {
     std::unique_ptr<khs::Engine> engine;
     bool built = false;
     uint32_t mode = KHSX_MODE_PLAIN_FP64;
+    uint32_t substep_limit = 0;
     std::vector<Vec> collider_pending;
     KhsBuildStats build_stats{};
     KhsStepStats step_stats{};
@@ -187,6 +188,7 @@ struct KhsSolver {
         }
         std::unique_ptr<khs::Engine> e(new khs::Engine());
         e->set_mode(mode);
+        e->set_substep_limit(substep_limit);
         e->initialize(model, desc, material, root_pos, root_rot);
         engine = std::move(e);
         collider_pending = model.collider;
@@ -609,6 +611,14 @@ KHS_API KhsResult khsxSetSolveMode(KhsSolver *s, uint32_t mode)
 }
 
 KHS_API uint32_t khsxGetSolveMode(const KhsSolver *s) { return s ? s->mode : 0; }
+
+KHS_API KhsResult khsxSetSubstepLimit(KhsSolver *s, uint32_t substeps)
+{
+    if (!s) return KHS_ERROR_INVALID_ARGUMENT;
+    s->substep_limit = substeps;
+    if (s->engine) s->engine->set_substep_limit(substeps);
+    return KHS_OK;
+}
 
 KHS_API KhsResult khsxSetRollbackRing(KhsSolver *s, uint32_t slots)
 {

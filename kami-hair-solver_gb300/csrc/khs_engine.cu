@@ -3173,15 +3173,17 @@ EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
     return s;
 }
 
-void Engine::limit_direction(double max_translation)
+bool Engine::limit_direction(double max_translation)
 {
     Impl &I = *d_;
     if (max_translation > trust_radius_) {
         I.launch("k_scale", k_scale, grid_for(6 * size_t(I.v.N)), kBlock, I.v, trust_radius_ / max_translation);
+        return true;
     }
+    return false;
 }
 
-void Engine::make_steepest()
+bool Engine::make_steepest()
 {
     Impl &I = *d_;
     I.launch("k_steepest", k_steepest, grid_for(6 * size_t(I.v.N)), kBlock, I.v);
@@ -3189,7 +3191,7 @@ void Engine::make_steepest()
     I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
     I.check();
     I.sync();
-    limit_direction(I.mail_host->max_translation);
+    return limit_direction(I.mail_host->max_translation);
 }
 
 // Launch shape of the persistent FP64 block solve: the layout (H = 1: five
@@ -3331,10 +3333,10 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
     const bool used = !mb.solve_failed && mb.slope < 0 && std::isfinite(mb.slope);
     if (!used) {
         ++rec.steepest_fallbacks;
-        make_steepest();
+        if (make_steepest()) ++rec.trust_scalings;
         return false;
     }
-    limit_direction(mb.max_translation);
+    if (limit_direction(mb.max_translation)) ++rec.trust_scalings;
     return true;
 }
 
@@ -3431,7 +3433,7 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
             if (!block_direction) break;
             KHS_CUDA(cudaMemcpyAsync(v.q, v.q_base, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
             ++rec.steepest_fallbacks;
-            make_steepest();
+            if (make_steepest()) ++rec.trust_scalings;
             block_direction = false;
         }
         if (!accepted) {
@@ -3500,6 +3502,7 @@ KhsResult Engine::run_frame(double frame_dt, const double *root_a, const double 
         bool crossed = false;
         KhsResult result = KHS_OK;
         for (uint32_t sub = 1; sub <= substeps; ++sub) {
+            if (substep_limit_ && sub > substep_limit_) break;
             progress_substep_.store(sub);
             progress_iteration_.store(0);
             KhsxSubstepRecord rec{};
@@ -3797,6 +3800,12 @@ KhsResult Engine::restore_checkpoint(const void *data, uint64_t size)
     KHS_CUDA(cudaMemcpyAsync(I.v.q_old, I.v.q, qb, cudaMemcpyDeviceToDevice, I.stream));
     KHS_CUDA(cudaMemcpyAsync(I.q_snap, I.v.q, qb, cudaMemcpyDeviceToDevice, I.stream));
     KHS_CUDA(cudaMemcpyAsync(I.v_snap, I.v.v, qb, cudaMemcpyDeviceToDevice, I.stream));
+    // The rollback ring must describe the restored trajectory: frames after
+    // the checkpoint's are forgotten, and the checkpoint's own frame is
+    // replaced by the restored state (the slot may hold another trajectory).
+    for (size_t j = 0; j < I.ring_frame.size(); ++j)
+        if (I.ring_frame[j] > int64_t(h.animation_frame)) I.ring_frame[j] = -1;
+    push_ring(h.animation_frame);
     I.sync();
     current_frame_ = h.animation_frame;
     drop_outputs_after(h.animation_frame);

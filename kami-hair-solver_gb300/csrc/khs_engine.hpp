@@ -86,6 +86,8 @@ public:
     KhsResult query_contacts_no_alloc(const double *q, uint64_t dof, KhsxContactRecord *out, uint32_t capacity);
 
     void set_mode(uint32_t mode) { mode_ = mode; }
+    // Ends every frame after its first `substeps` substeps (0: whole frames).
+    void set_substep_limit(uint32_t substeps) { substep_limit_ = substeps; }
     // Block-solve launch shape: 5, 2 or 1 strands per warp and blocks of four
     // warps per SM (long_strands > 0 with 5: the longest strands one per
     // warp first); 0 strands per warp restores the one-time tuning.
@@ -127,12 +129,13 @@ private:
     void tune_block_solve();
     void launch_block_solve();
     void push_ring(uint32_t frame);
-    void make_steepest();
-    void limit_direction(double max_translation);
+    // Both return whether the trust radius scaled the direction.
+    bool make_steepest();
+    bool limit_direction(double max_translation);
 
     KhsSolverDesc desc_{};
     KhsHairMaterial material_{};
-    uint32_t mode_ = 0;
+    uint32_t mode_ = 0, substep_limit_ = 0;
     bool initialized_ = false, animation_ready_ = false;
     uint32_t animation_frames_ = 0, current_frame_ = 0;
     std::vector<bool> root_frame_set_, collider_frame_set_;

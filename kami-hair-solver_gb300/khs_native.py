@@ -139,7 +139,7 @@ class SubstepRecord(ctypes.Structure):
     _fields_ = [
         ("struct_size", c_u32), ("substep", c_u32), ("newton_iterations", c_u32),
         ("line_search_evaluations", c_u32), ("steepest_fallbacks", c_u32), ("refinement_sweeps", c_u32),
-        ("fp64_fallbacks", c_u32), ("reserved", c_u32), ("contact_candidates", c_u64), ("active_contacts", c_u64), ("final_residual_norm", c_f64),
+        ("fp64_fallbacks", c_u32), ("trust_scalings", c_u32), ("contact_candidates", c_u64), ("active_contacts", c_u64), ("final_residual_norm", c_f64),
         ("minimum_gap", c_f64),
     ]
 
@@ -200,6 +200,7 @@ ABI_FUNCTIONS = [
 EXTENSION_FUNCTIONS = [
     ("khsxSetSolveMode", ctypes.c_int, [VP, c_u32]),
     ("khsxGetSolveMode", c_u32, [VP]),
+    ("khsxSetSubstepLimit", ctypes.c_int, [VP, c_u32]),
     ("khsxCopyState", ctypes.c_int, [VP, VP, VP, c_u64]),
     ("khsxGetSubstepRecordCount", c_u32, [VP]),
     ("khsxCopySubstepRecords", ctypes.c_int, [VP, P(SubstepRecord), c_u32]),
@@ -451,6 +452,11 @@ class HairSolver:
     # -- GB300 extensions -------------------------------------------------
     def set_solve_mode(self, mode: int):
         self._check(self._library.khsxSetSolveMode(self._handle, int(mode)))
+
+    def set_substep_limit(self, substeps: int):
+        """khsxSetSubstepLimit: end every following frame after ``substeps``
+        substeps (0: whole frames)."""
+        self._check(self._library.khsxSetSubstepLimit(self._handle, int(substeps)))
 
     def state(self) -> tuple[np.ndarray, np.ndarray]:
         n = int(self._library.khsGetInternalNodeCount(self._handle))

@@ -831,6 +831,61 @@ public:
                 strands[3 * s] = strands_[s].first; strands[3 * s + 1] = strands_[s].count; strands[3 * s + 2] = strands_[s].fixed_count;
             }
     }
+    // Test hook: the built rod model in the form the reference's CUDA backend
+    // takes it (CudaNodeInit / CudaElementInit / strand node lists, the
+    // original-to-internal map and the collider; cuda_backend.hpp:14-55,
+    // filled as solver.cpp:485-517 fills them).  sizes = {nodes, elements,
+    // strands, original points, collider vertices, triangles}.  Per node:
+    // 18 doubles (position, rotation vector, reference frame rows 0-2, mass,
+    // rotational mass, binding t) and 4 u32 (strand, binding left, binding
+    // right, fixed).  Per element: 7 doubles (rest length, rest shear, rest
+    // curvature) and 4 u32 (i, j, strand, collider contact).  Per strand: its
+    // first node and node count (the nodes of a strand are consecutive).
+    void model_sizes(uint32_t *sizes) const
+    {
+        sizes[0] = uint32_t(nodes_.size()); sizes[1] = uint32_t(elements_.size());
+        sizes[2] = uint32_t(strand_nodes_.size()); sizes[3] = uint32_t(mapping_.size());
+        sizes[4] = has_collider_ ? uint32_t(collider_current_.size()) : 0u;
+        sizes[5] = has_collider_ ? uint32_t(triangles_.size()) : 0u;
+    }
+    void export_model(double *node_f, uint32_t *node_u, double *elem_f, uint32_t *elem_u, uint32_t *strand_u,
+                      uint32_t *mapping, double *collider, uint32_t *tris) const
+    {
+        for (size_t i = 0; i < nodes_.size(); ++i) {
+            const Node &n = nodes_[i];
+            double *f = node_f + 18 * i;
+            f[0] = n.x.x; f[1] = n.x.y; f[2] = n.x.z;
+            f[3] = n.rotation.x; f[4] = n.rotation.y; f[5] = n.rotation.z;
+            for (int k = 0; k < 9; ++k) f[6 + k] = n.ref.m[k];
+            f[15] = n.mass; f[16] = n.rmass; f[17] = n.binding.t;
+            uint32_t *u = node_u + 4 * i;
+            u[0] = n.strand; u[1] = n.binding.left; u[2] = n.binding.right; u[3] = n.fixed ? 1u : 0u;
+        }
+        for (size_t e = 0; e < elements_.size(); ++e) {
+            const Element &el = elements_[e];
+            double *f = elem_f + 7 * e;
+            f[0] = el.L0;
+            f[1] = el.rest_shear.x; f[2] = el.rest_shear.y; f[3] = el.rest_shear.z;
+            f[4] = el.rest_curv.x; f[5] = el.rest_curv.y; f[6] = el.rest_curv.z;
+            uint32_t *u = elem_u + 4 * e;
+            u[0] = el.i; u[1] = el.j; u[2] = el.strand; u[3] = el.contact ? 1u : 0u;
+        }
+        for (size_t s = 0; s < strand_nodes_.size(); ++s) {
+            strand_u[2 * s] = strand_nodes_[s].front();
+            strand_u[2 * s + 1] = uint32_t(strand_nodes_[s].size());
+        }
+        std::copy(mapping_.begin(), mapping_.end(), mapping);
+        if (has_collider_) {
+            for (size_t v = 0; v < collider_current_.size(); ++v) {
+                collider[3 * v] = collider_current_[v].x; collider[3 * v + 1] = collider_current_[v].y;
+                collider[3 * v + 2] = collider_current_[v].z;
+            }
+            for (size_t t = 0; t < triangles_.size(); ++t) {
+                tris[3 * t] = triangles_[t].i0; tris[3 * t + 1] = triangles_[t].i1; tris[3 * t + 2] = triangles_[t].i2;
+            }
+        }
+    }
+    void set_substep_limit(uint32_t n) { substep_limit_ = n; }
     uint32_t record_count() const { return uint32_t(records_.size()); }
     KhsResult copy_records(KhsxSubstepRecord *out, uint32_t cap) const
     {
@@ -1508,6 +1563,7 @@ private:
         if (mx > trust_radius_) {
             const double scale = trust_radius_ / mx;
             for (double &x : dir_) x *= scale;
+            ++trust_;
         }
     }
 
@@ -1812,6 +1868,7 @@ private:
             KhsResult result = KHS_OK;
             for (uint32_t sub = 1; sub <= substeps; ++sub) {
                 if (g_substep_limit && sub > g_substep_limit) break;
+                if (substep_limit_ && sub > substep_limit_) break;
                 progress_substep_.store(sub);
                 progress_iteration_.store(0);
                 KhsxSubstepRecord rec{};
@@ -1819,6 +1876,7 @@ private:
                 rec.substep = sub;
                 rec.minimum_gap = std::numeric_limits<double>::infinity();
                 steepest_ = 0;
+                trust_ = 0;
                 old_q_ = q_;
                 const double f = double(sub) / substeps;
                 for (size_t n = 0; n < N(); ++n) {
@@ -1852,6 +1910,7 @@ private:
                 progress_phase_.store(KHS_PHASE_ASSEMBLING);
                 result = optimize_substep(dt, rec);
                 rec.steepest_fallbacks = steepest_;
+                rec.trust_scalings = trust_;
                 records_.push_back(rec);
                 if (result != KHS_OK) {
                     if (!cancel_.load()) {
@@ -1913,7 +1972,8 @@ private:
     std::vector<ElemOut> elem_out_;
     std::vector<KhsxContactRecord> contact_records_;
     std::vector<KhsxSubstepRecord> records_;
-    uint32_t steepest_ = 0;
+    uint32_t substep_limit_ = 0;  // khsxSetSubstepLimit (0: whole frames)
+    uint32_t steepest_ = 0, trust_ = 0;  // per substep: steepest fallbacks, trust-radius scalings
     double max_rest_length_ = 0.0, trust_radius_ = 0.0, last_frame_ms_ = 0.0;
     bool animation_ready_ = false;
     uint32_t anim_frames_ = 0, current_frame_ = 0;
@@ -2053,6 +2113,12 @@ KHS_API const char *khsGetLastError(const KhsSolver *s)
 
 KHS_API KhsResult khsxSetSolveMode(KhsSolver *s, uint32_t mode) { return s && mode <= 2 ? KHS_OK : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API uint32_t khsxGetSolveMode(const KhsSolver *) { return 0; }
+KHS_API KhsResult khsxSetSubstepLimit(KhsSolver *s, uint32_t n)
+{
+    if (!s) return KHS_ERROR_INVALID_ARGUMENT;
+    s->impl.set_substep_limit(n);
+    return KHS_OK;
+}
 KHS_API KhsResult khsxCopyState(const KhsSolver *s, double *q, double *v, uint64_t cap) { return s ? s->impl.copy_state(q, v, cap) : KHS_ERROR_INVALID_ARGUMENT; }
 KHS_API uint32_t khsxGetSubstepRecordCount(const KhsSolver *s) { return s ? s->impl.record_count() : 0; }
 KHS_API KhsResult khsxCopySubstepRecords(const KhsSolver *s, KhsxSubstepRecord *r, uint32_t c) { return s ? s->impl.copy_records(r, c) : KHS_ERROR_INVALID_ARGUMENT; }
@@ -2065,6 +2131,18 @@ KHS_API KhsResult khsxComputeRootTargets(KhsSolver *s, const KhsVec3 *p, uint32_
 KHS_API void khsOracleExportSystem(const KhsSolver *s, double *diag, double *upper, double *grad, uint32_t *strands)
 {
     if (s) s->impl.export_system(diag, upper, grad, strands);
+}
+
+// Oracle-only test hooks (see Solver::model_sizes / export_model): the built
+// model as the reference's CUDA backend takes it.
+KHS_API void khsOracleModelSizes(const KhsSolver *s, uint32_t *sizes)
+{
+    if (s && sizes) s->impl.model_sizes(sizes);
+}
+KHS_API void khsOracleExportModel(const KhsSolver *s, double *node_f, uint32_t *node_u, double *elem_f, uint32_t *elem_u,
+                                  uint32_t *strand_u, uint32_t *mapping, double *collider, uint32_t *tris)
+{
+    if (s) s->impl.export_model(node_f, node_u, elem_f, elem_u, strand_u, mapping, collider, tris);
 }
 
 // Oracle-only: stop every frame after n substeps (0 = whole frames).

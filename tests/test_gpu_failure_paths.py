@@ -1,0 +1,160 @@
+"""Failure-side branches on the GB300 library, against the CPU oracle and,
+where its sources are staged, the reference's own CUDA backend:
+
+* the line search that can take no trial (NONLINEAR_SOLVE) and the start
+  outside the barrier's feasible region (BARRIER_INFEASIBLE) give the
+  reference's result code and the oracle's failure diagnostics field for
+  field, with the frame-start state restored;
+* khsRequestCancel from a second thread stops the frame with
+  KHS_ERROR_INVALID_STATE and restores its start state;
+* the steepest-descent retry and the trust-radius scaling: scenes that take
+  them many times keep parity with the oracle (identical per-substep counts
+  of Newton iterations, line-search trials, steepest retries and trust
+  scalings; positions within 1e-6 m, rotations within 1e-6 rad)."""
+import numpy as np
+import pytest
+
+import failure_cases as fc
+import khs_native as kn
+import parity
+import refgpu
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+DIAG_FIELDS = ["kind", "frame_index", "substep", "requested_substeps", "attempted_substeps", "maximum_substeps",
+               "adaptive_attempt_count", "strand_index", "element_index", "collider_triangle_index"]
+
+
+def _solver(lib, scene, mode=None):
+    s = kn.HairSolver(lib)
+    scenes.load_into(s, scene)
+    if mode is not None:
+        s.set_solve_mode(mode)
+    return s
+
+
+def _diag(d):
+    return {f: getattr(d, f) for f in DIAG_FIELDS}
+
+
+@pytest.mark.parametrize("mode", [kn.MODE_PLAIN_FP64, kn.MODE_MIXED])
+def test_line_search_exhausted(gpu_lib, oracle_lib, mode):
+    sc = fc.line_search_exhausted()
+    out = []
+    for lib, m in ((gpu_lib, mode), (oracle_lib, None)):
+        s = _solver(lib, sc, m)
+        before = s.save_checkpoint()
+        r = s._library.khsStepAnimationFrame(s.handle, 1, sc.frame_dt)
+        out.append((r, _diag(s.failure_diagnostics()), s.save_checkpoint() == before))
+        s.close()
+    assert out[0] == out[1]
+    assert out[0][0] == kn.ERROR_NOT_CONVERGED and out[0][1]["kind"] == kn.FAILURE_NONLINEAR_SOLVE and out[0][2]
+
+
+@pytest.mark.parametrize("mode", [kn.MODE_PLAIN_FP64, kn.MODE_MIXED])
+def test_infeasible_start(gpu_lib, oracle_lib, mode):
+    sc = fc.infeasible_scene()
+    out = []
+    for lib, m in ((gpu_lib, mode), (oracle_lib, None)):
+        s = _solver(lib, sc, m)
+        bad = fc.infeasible_checkpoint(s.save_checkpoint(), sc)
+        s.restore_checkpoint(bad)
+        r = s._library.khsStepAnimationFrame(s.handle, 1, sc.frame_dt)
+        out.append((r, _diag(s.failure_diagnostics()), s.save_checkpoint() == bad))
+        s.close()
+    assert out[0] == out[1]
+    assert out[0][0] == kn.ERROR_NOT_CONVERGED and out[0][1]["kind"] == kn.FAILURE_BARRIER_INFEASIBLE and out[0][2]
+
+
+@pytest.mark.parametrize("mode", [kn.MODE_PLAIN_FP64, kn.MODE_MIXED])
+def test_cancel_from_another_thread(gpu_lib, mode):
+    sc = scenes.ellipsoid_scene(strands=1000, frames=1)
+    s = _solver(gpu_lib, sc, mode)
+    before = s.save_checkpoint()
+    r = fc.cancel_mid_frame(lambda: s._library.khsStepAnimationFrame(s.handle, 1, sc.frame_dt), s.progress, s.cancel)
+    assert r == kn.ERROR_INVALID_STATE
+    assert s.progress().cancelled == 1
+    assert s.failure_diagnostics().kind == kn.FAILURE_NONE
+    assert s.save_checkpoint() == before
+    assert s._library.khsStepAnimationFrame(s.handle, 1, sc.frame_dt) == kn.OK
+    again = s.save_checkpoint()
+    s.close()
+    t = _solver(gpu_lib, sc, mode)
+    assert t._library.khsStepAnimationFrame(t.handle, 1, sc.frame_dt) == kn.OK
+    assert t.save_checkpoint() == again
+    t.close()
+
+
+def _record_counts(frames):
+    return [[(r.newton_iterations, r.line_search_evaluations, r.steepest_fallbacks, r.trust_scalings,
+              r.contact_candidates, r.active_contacts) for r in fr["records"]] for fr in frames]
+
+
+@pytest.mark.parametrize("make,field", [(fc.steepest_heavy, "steepest_fallbacks"), (fc.root_jump, "trust_scalings")])
+@pytest.mark.parametrize("mode", [kn.MODE_PLAIN_FP64, kn.MODE_MIXED])
+def test_fallback_branches_keep_parity(gpu_lib, oracle_lib, make, field, mode):
+    gpu = parity.run(gpu_lib, make(), mode=mode)
+    ora = parity.run(oracle_lib, make())
+    assert _record_counts(gpu) == _record_counts(ora)
+    assert sum(getattr(r, field) for fr in gpu for r in fr["records"]) > 0
+    for k, fr in enumerate(parity.compare(gpu, ora)):
+        assert fr["result"] == (kn.OK, kn.OK), (k, fr)
+        assert fr["max_position"] <= TOL and fr["max_rotation"] <= TOL, (k, fr)
+
+
+# ---- the reference's own CUDA backend ---------------------------------------
+
+@pytest.fixture(scope="module")
+def ref_lib():
+    if not refgpu.available():
+        pytest.skip("the reference CUDA sources are not staged in oracle/_ref/src")
+    return refgpu.RefLibrary()
+
+
+def test_reference_failure_codes(ref_lib, oracle_lib):
+    """The reference backend gives the same result codes and failure kinds
+    on the same two failing frames."""
+    sc = fc.line_search_exhausted()
+    s = refgpu.RefSolver(ref_lib, oracle_lib, sc)
+    before = s.save_checkpoint()
+    assert s.step_animation_frame(1, sc.frame_dt) == kn.ERROR_NOT_CONVERGED
+    d = s.failure()
+    assert (d.kind, d.substep, d.attempted_substeps, d.adaptive_attempt_count) == (kn.FAILURE_NONLINEAR_SOLVE, 1, 32, 4)
+    assert s.save_checkpoint() == before
+    s.close()
+    sc = fc.infeasible_scene()
+    s = refgpu.RefSolver(ref_lib, oracle_lib, sc)
+    bad = fc.infeasible_checkpoint(s.save_checkpoint(), sc)
+    s.restore_checkpoint(bad)
+    assert s.step_animation_frame(1, sc.frame_dt) == kn.ERROR_NOT_CONVERGED
+    assert s.failure().kind == kn.FAILURE_BARRIER_INFEASIBLE
+    assert s.save_checkpoint() == bad
+    s.close()
+
+
+def test_reference_cancel(ref_lib, oracle_lib):
+    sc = scenes.ellipsoid_scene(strands=1000, frames=1)
+    s = refgpu.RefSolver(ref_lib, oracle_lib, sc)
+    before = s.save_checkpoint()
+    r = fc.cancel_mid_frame(lambda: s.step_animation_frame(1, sc.frame_dt), s.progress, s.cancel)
+    assert r == kn.ERROR_INVALID_STATE
+    assert s.save_checkpoint() == before
+    s.close()
+
+
+@pytest.mark.parametrize("make", [fc.steepest_heavy, fc.root_jump])
+def test_reference_fallback_branches(ref_lib, oracle_lib, make):
+    """The GB300 library against the reference backend on the fallback-heavy
+    scenes: same result codes, Newton and line-search counts, and states
+    within the tolerance (the reference sums with atomics, so its own runs
+    differ in the last bits)."""
+    ref = refgpu.run(ref_lib, oracle_lib, make())
+    ora = parity.run(oracle_lib, make())
+    for k, (a, b) in enumerate(zip(ref, ora)):
+        assert a["result"] == b["result"] == kn.OK, k
+        assert a["stats"].newton_iterations == b["stats"].newton_iterations, k
+        assert a["stats"].line_search_evaluations == b["stats"].line_search_evaluations, k
+        dq = np.abs(a["q"] - b["q"])
+        assert dq[:, :3].max() <= TOL and dq[:, 3:].max() <= TOL, (k, dq[:, :3].max(), dq[:, 3:].max())

@@ -44,3 +44,32 @@ def test_rollback_ring_restores_frames(gpu_lib):
     q, v = s.state()
     assert np.array_equal(q, states[2][0]) and np.array_equal(v, states[2][1])
     s.close()
+
+
+def test_restored_checkpoint_resets_rollback_ring(gpu_lib):
+    """Restoring a checkpoint forgets the ring's later frames and puts the
+    restored state in the checkpoint frame's slot."""
+    sc = scenes.sphere_scene(motion=True, frames=6)
+    s = kn.HairSolver(gpu_lib)
+    scenes.load_into(s, sc)
+    s.set_rollback_ring(6)
+    checkpoints = {}
+    for f in range(1, 6):
+        assert s._library.khsStepAnimationFrame(s.handle, f, sc.frame_dt) == kn.OK
+        checkpoints[f] = s.save_checkpoint()
+    s.restore_checkpoint(checkpoints[2])
+    assert s._library.khsxRollbackToFrame(s.handle, 4) == kn.ERROR_INVALID_ARGUMENT
+    assert s._library.khsxRollbackToFrame(s.handle, 3) == kn.ERROR_INVALID_ARGUMENT
+    s.rollback_to_frame(2)
+    assert s.save_checkpoint() == checkpoints[2]
+    # A checkpoint from another trajectory: its state, not the ring's, is frame 2's.
+    other = bytearray(checkpoints[2])
+    header = 24
+    q = np.frombuffer(bytes(other[header:]), dtype=np.float64).copy()
+    q[len(q) // 2 - 1] += 1e-9  # the last node's rotation z (q, then v)
+    other[header:] = q.tobytes()
+    s.restore_checkpoint(bytes(other))
+    assert s._library.khsStepAnimationFrame(s.handle, 3, sc.frame_dt) == kn.OK
+    s.rollback_to_frame(2)
+    assert s.save_checkpoint() == bytes(other)
+    s.close()
