@@ -12,28 +12,45 @@ Prints ONE JSON line (rank 0).  ``value`` is the mixed form (FP32 filters,
 results identical to the plain form); the plain FP64 form is timed on the
 same frames and reported beside it as ``plain_fp64``.  Keys beyond the base
 contract:
-* roofline     -- the dominant kernel (largest share of device time in the
-                  timed region): algorithmic bytes per launch / its average
-                  CUDA-event duration measured live, against the measured HBM
-                  copy bandwidth; ``fp64`` adds algorithmic FP64 flops per
-                  launch against the FMA-pipe rate measured on this GPU by
-                  khsxMeasurePipePeaks (the heavy kernels are FP64-pipe
-                  bound).  ``traffic`` is DRAM bytes per launch from the ncu
-                  capture summarised under profiles/.
+* roofline     -- the dominant kernel (largest share of device time in an
+                  untimed re-run of the first timed frames with per-kernel
+                  CUDA-event timing; the timed frames run without it):
+                  algorithmic bytes per launch / average launch time against
+                  the measured HBM copy bandwidth, and, where the kernel has
+                  an algorithmic FP64 flop count, flops per launch against
+                  the FMA-pipe rate measured on this GPU by
+                  khsxMeasurePipePeaks; ``bound`` names the closer roof.
+                  ``traffic`` is DRAM bytes per launch from the ncu capture
+                  summarised under profiles/.
+* host_gap     -- device time of those frames against the sum of their
+                  kernels' times: the share the GPU waits on the host.
 * cpu_baseline -- the CPU oracle (a port of the reference method; the
-                  reference has no CPU solver) on this host's cores, on a
-                  bounded sample of the same workload.
+                  reference has no CPU solver) on this host's cores, on the
+                  first substeps of the first timed frame from the timed
+                  region's GB300 checkpoint.
+* same_sample  -- both GB300 forms on exactly those substeps from the same
+                  checkpoint: rate, and the maximum position and rotation
+                  deviation from the oracle (also max_position_dev_m and
+                  max_rotation_dev_rad at the top level, for the mixed form).
+* reference_gpu - the reference's own FP64 CUDA backend (its
+                  src/cuda_backend.cu built unchanged for sm_103a from the
+                  sources staged in oracle/_ref) on the first timed frames
+                  from the same checkpoint, beside the mixed form's rate on
+                  those frames.
 * e2e          -- the same metric through the public C ABI with host
                   buffers: khsUpdateRootTargets + khsUpdateColliderVertices
                   (pinned host arrays) + khsStep + khsCopyOriginalPositions
                   every step, wall clock.
 * clocks       -- nvidia-smi samples taken during the timed region.
 
+The baseline legs (cpu_baseline, same_sample's oracle, reference_gpu) are
+the only code here that runs anything under oracle/.
+
 ``--impl reference`` times the CPU oracle (the reference method restated;
-the reference ships no CPU implementation and its CUDA sources do not travel
-to this machine) on all host threads, each step one substep of the same
-workload.  ``--gpus N`` under torchrun runs N independent replicas (the solve
-does not exchange data between strands' GPUs): weak scaling.
+the reference ships no CPU implementation) on all host threads, each step
+the first substeps of one frame of the same workload.  ``--gpus N`` under
+torchrun runs N independent replicas (the solve does not exchange data
+between strands' GPUs): weak scaling.
 """
 from __future__ import annotations
 
@@ -216,6 +233,102 @@ def cpu_oracle_sample(scene, full_frames: int, repeats: int, substeps: int, thre
                       f"{cores} threads"}
 
 
+def oracle_sample_from(scene, checkpoint: bytes, frame: int, substeps: int, repeats: int,
+                       threads: int | None = None) -> dict:
+    """Times the CPU oracle on the first ``substeps`` substeps of ``frame``,
+    starting every repeat from ``checkpoint`` (the GB300 state after frame
+    ``frame - 1``); returns the rate and the state reached."""
+    import khs_native as kn
+    import scenes
+
+    lib = _oracle_library()
+    cores = int(lib.lib.khsOracleSetThreads(threads or os.cpu_count() or 1))
+    lib.lib.khsOracleSetSubstepLimit(0)
+    s = kn.HairSolver(lib)
+    scenes.load_into(s, scene, frames=frame + 1)
+    s.set_substep_limit(substeps)
+    done, newton, seconds, per_step = 0, 0, 0.0, []
+    for _ in range(repeats):
+        s.restore_checkpoint(checkpoint)
+        t0 = time.perf_counter()
+        r = s._library.khsStepAnimationFrame(s.handle, frame, scene.frame_dt)
+        dt = time.perf_counter() - t0
+        if r != kn.OK:
+            raise RuntimeError(f"oracle frame {frame} failed ({r}): {s.last_error()}")
+        st = s.stats()
+        done += st.converged_substeps
+        newton += st.newton_iterations
+        seconds += dt
+        per_step.append(dt)
+    q = s.state()[0]
+    s.close()
+    return {"value": done / seconds, "unit": UNIT, "cores": cores, "kind": "port", "seconds": seconds,
+            "substeps": done, "newton_iterations": newton, "per_step_s": per_step, "q": q,
+            "sample": f"first {substeps} substeps of frame {frame} of the same body scene, {repeats} run(s) from "
+                      f"the GB300 checkpoint after frame {frame - 1}; CPU FP64 oracle on {cores} threads"}
+
+
+def gpu_sample_from(lib, scene, checkpoint: bytes, frame: int, substeps: int, mode: int) -> dict:
+    """The GB300 library on exactly the oracle sample's substeps (same
+    checkpoint, same substep limit); device time of the second run (the
+    first also tunes the block-solve launch shape)."""
+    import khs_native as kn
+    import scenes
+
+    s = kn.HairSolver(lib)
+    scenes.load_into(s, scene, frames=frame + 1)
+    s.set_solve_mode(mode)
+    s.set_substep_limit(substeps)
+    for _ in range(2):
+        s.restore_checkpoint(checkpoint)
+        if s._library.khsStepAnimationFrame(s.handle, frame, scene.frame_dt) != kn.OK:
+            raise RuntimeError(f"sampled frame {frame} failed: {s.last_error()}")
+    ms = s.gpu_stats().last_frame_milliseconds
+    st = s.stats()
+    q = s.state()[0]
+    s.close()
+    return {"value": st.converged_substeps / (ms / 1e3), "unit": UNIT, "device_ms": ms,
+            "substeps": int(st.converged_substeps), "newton_iterations": int(st.newton_iterations), "q": q}
+
+
+def reference_gpu_frames(scene, checkpoint: bytes, first: int, count: int, frame_ms: list, frame_substeps: list) -> dict:
+    """The reference's own FP64 CUDA backend (its src/cuda_backend.cu built
+    unchanged for sm_103a, oracle/_ref) on frames first..first+count-1 of the
+    same scene from the same checkpoint as the timed frames; beside it the
+    mixed form's rate on those frames, from the timed run."""
+    sys.path.append(str(REPO / "oracle"))
+    import refgpu
+
+    if not refgpu.available():
+        return {"unavailable": "the reference CUDA sources are not staged in oracle/_ref/src"}
+    ref = refgpu.RefLibrary()
+    s = refgpu.RefSolver(ref, _oracle_library(), scene, frames=first + count)
+    s.restore_checkpoint(checkpoint)  # module load and first launches outside the timing
+    if s.step_animation_frame(first, scene.frame_dt) != 0:
+        raise RuntimeError(f"reference frame {first} failed: {s.last_error()}")
+    s.restore_checkpoint(checkpoint)
+    wall, device, substeps, newton = [], [], [], 0
+    for f in range(first, first + count):
+        t0 = time.perf_counter()
+        r = s.step_animation_frame(f, scene.frame_dt)
+        wall.append(time.perf_counter() - t0)
+        if r != 0:
+            raise RuntimeError(f"reference frame {f} failed ({r}): {s.last_error()}")
+        device.append(s.gpu_stats().last_frame_milliseconds)
+        st = s.stats()
+        substeps.append(int(st.substeps))
+        newton += st.newton_iterations
+    s.close()
+    ours_s = sum(frame_ms[:count]) / 1e3
+    return {"value": sum(substeps) / sum(wall), "unit": UNIT, "frames": f"{first}-{first + count - 1}",
+            "substeps": substeps, "newton_iterations": newton, "frame_ms": [round(1e3 * w, 1) for w in wall],
+            "event_ms": [round(x, 1) for x in device],
+            "mixed_same_frames": {"value": sum(frame_substeps[:count]) / ours_s, "substeps": frame_substeps[:count]},
+            "note": "the reference's src/cuda_backend.cu compiled unchanged for sm_103a, FP64, stepped from the "
+                    "GB300 checkpoint of the timed region's start; its substep counts may differ from ours because "
+                    "it sums with atomics"}
+
+
 def run_reference(args) -> None:
     world, rank = _dist()
     if rank != 0:
@@ -247,9 +360,12 @@ def _config(scene, mode: str) -> dict:
             "mode": mode, "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
 
 
-def time_frames(lib, scene, mode: int, args, torch, flush, world: int) -> dict:
+def time_frames(lib, scene, mode: int, args, torch, flush, world: int, profile_frames: int) -> dict:
     """Warm-up frames, then the timed frames of one solve mode (device time
-    of each frame from the library's CUDA events, per-kernel timings on)."""
+    of each frame from the library's CUDA events, no per-kernel timing).
+    Afterwards, untimed, the first ``profile_frames`` timed frames are run
+    again from a checkpoint of the timed region's start with per-kernel
+    CUDA-event timing on, for the kernel shares and the roofline."""
     import khs_native as kn
     import scenes
 
@@ -259,15 +375,14 @@ def time_frames(lib, scene, mode: int, args, torch, flush, world: int) -> dict:
     solver.set_solve_mode(mode)
     for f in range(1, args.warmup + 1):
         solver.step_animation_frame(f, scene.frame_dt)
-    solver.set_profiling(True)
-    solver.reset_kernel_timings()
+    start = solver.save_checkpoint()
     launches0 = solver.kernel_launches()
     clocks = ClockSampler()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    frame_ms, substeps, newton, candidates = [], 0, 0, 0
+    frame_ms, frame_substeps, newton, candidates = [], [], 0, 0
     wall0 = time.perf_counter()
     for f in range(args.warmup + 1, frames):
         _flush_l2(torch, flush)
@@ -276,19 +391,35 @@ def time_frames(lib, scene, mode: int, args, torch, flush, world: int) -> dict:
             raise RuntimeError(f"frame {f} failed ({r}): {solver.last_error()}")
         frame_ms.append(solver.gpu_stats().last_frame_milliseconds)
         st = solver.stats()
-        substeps += st.substeps
+        frame_substeps.append(int(st.substeps))
         newton += st.newton_iterations
         candidates += st.contact_candidate_count
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     clock_info = clocks.stop()
+    launches = solver.kernel_launches() - launches0
     import replicas
 
-    out = {"device_s": sum(frame_ms) / 1e3, "wall_s": wall, "substeps": substeps, "newton": newton,
-           "candidates": candidates, "frame_ms": frame_ms, "clocks": clock_info,
-           "launches": solver.kernel_launches() - launches0, "timings": solver.kernel_timings(),
-           "stats": solver.build_stats(), "checksum": replicas.state_checksum(solver.state()[0])}
+    checksum = replicas.state_checksum(solver.state()[0])
+    # Untimed profiling pass over the same frames.
+    solver.restore_checkpoint(start)
+    solver.set_profiling(True)
+    solver.reset_kernel_timings()
+    profiled_ms, profiled_candidates = [], 0
+    for f in range(args.warmup + 1, args.warmup + 1 + profile_frames):
+        _flush_l2(torch, flush)
+        if solver._library.khsStepAnimationFrame(solver.handle, f, scene.frame_dt) != kn.OK:
+            raise RuntimeError(f"profiled frame {f} failed: {solver.last_error()}")
+        profiled_ms.append(solver.gpu_stats().last_frame_milliseconds)
+        profiled_candidates += solver.stats().contact_candidate_count
+    timings = solver.kernel_timings()
     solver.set_profiling(False)
+    out = {"device_s": sum(frame_ms) / 1e3, "wall_s": wall, "substeps": sum(frame_substeps), "newton": newton,
+           "candidates": candidates, "frame_ms": frame_ms, "frame_substeps": frame_substeps, "clocks": clock_info,
+           "launches": launches, "timings": timings, "profiled_frames": profile_frames,
+           "profiled_ms": profiled_ms, "profiled_candidates": profiled_candidates,
+           "kernel_ms_sum": sum(ms for _, ms in timings.values()),
+           "stats": solver.build_stats(), "checksum": checksum, "start_checkpoint": start}
     solver.close()
     return out
 
@@ -304,6 +435,13 @@ def _aggregate(run: dict, world: int) -> dict:
 
 
 def _roofline(run: dict, fp64_peak: float) -> dict:
+    """Roofline of the kernel with the largest share of device time in the
+    profiled frames.  Its algorithmic bytes per launch over its average
+    launch time, against the measured HBM copy bandwidth; where the kernel
+    has an algorithmic FP64 flop count, also its flops per launch against the
+    FP64 FMA-pipe rate measured on this GPU.  ``bound`` names the roof the
+    kernel is closer to, and the top-level achieved / peak / frac are that
+    roof's; the other roof is kept under ``hbm`` or ``fp64``."""
     timings = run["timings"]
     total = sum(ms for _, ms in timings.values()) or 1.0
     name, (count, ms) = max(timings.items(), key=lambda kv: kv[1][1]) if timings else ("none", (0, 0.0))
@@ -311,7 +449,7 @@ def _roofline(run: dict, fp64_peak: float) -> dict:
     nodes, elements = int(st.internal_node_count), int(st.element_count)
     free_nodes = nodes - int(st.fixed_node_count)
     grad_evals = timings.get("k_elem_eval_grad", (0, 0.0))[0] or 1
-    cand_per_eval = run["candidates"] / grad_evals
+    cand_per_eval = run["profiled_candidates"] / grad_evals
     per_launch_s = (ms / max(count, 1)) / 1e3
     alg_bytes, alg_flops = algorithmic(name, nodes, free_nodes, elements, cand_per_eval)
     peaks = json.loads(MEASURED_PEAKS.read_text()) if MEASURED_PEAKS.exists() else {}
@@ -322,18 +460,37 @@ def _roofline(run: dict, fp64_peak: float) -> dict:
         # copy measurement on a GB300.
         hbm_peak, peak_source = 6800.0, "fallback (6.8 TB/s, an earlier copy measurement on a GB300)"
     achieved = alg_bytes / per_launch_s / 1e9 if (alg_bytes and per_launch_s > 0) else None
-    roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak if (achieved and hbm_peak) else None,
-            "traffic": NCU_TRAFFIC_BYTES.get(name), "algorithmic_bytes_per_launch": alg_bytes,
-            "peak_source": peak_source,
-            "avg_launch_ms": ms / max(count, 1), "launches": count, "share": ms / total,
-            "kernel_shares": {k: round(v[1] / total, 4) for k, v in sorted(timings.items(), key=lambda kv: -kv[1][1])}}
+    hbm = {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+           "frac": achieved / hbm_peak if (achieved and hbm_peak) else None, "peak_source": peak_source,
+           "algorithmic_bytes_per_launch": alg_bytes}
+    fp64 = None
     if alg_flops:
         tf = alg_flops / per_launch_s / 1e12
-        roof["fp64"] = {"achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": tf / fp64_peak,
-                        "algorithmic_flops_per_launch": alg_flops,
-                        "peak_source": "measured FP64 FMA-pipe rate of this GPU (khsxMeasurePipePeaks)"}
+        fp64 = {"achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": tf / fp64_peak,
+                "algorithmic_flops_per_launch": alg_flops,
+                "peak_source": "measured FP64 FMA-pipe rate of this GPU (khsxMeasurePipePeaks)"}
+    bound = "fp64" if fp64 and (hbm["frac"] or 0.0) < fp64["frac"] else "hbm"
+    top = fp64 if bound == "fp64" else hbm
+    roof = {"bound": bound, "kernel": name, "achieved": top["achieved"], "peak": top["peak"], "unit": top["unit"],
+            "frac": top["frac"], "traffic": NCU_TRAFFIC_BYTES.get(name), "algorithmic_bytes_per_launch": alg_bytes,
+            "avg_launch_ms": ms / max(count, 1), "launches": count, "share": ms / total,
+            "profiled_frames": run["profiled_frames"],
+            "kernel_shares": {k: round(v[1] / total, 4) for k, v in sorted(timings.items(), key=lambda kv: -kv[1][1])}}
+    if bound == "fp64":
+        roof["hbm"] = hbm
+    elif fp64:
+        roof["fp64"] = fp64
     return roof
+
+
+def _host_gap(run: dict) -> dict:
+    """Device time of the profiled frames against the sum of their kernels'
+    CUDA-event times: the difference is time the GPU waited on the host
+    (launch gaps and the host-driven Newton loop's synchronisations)."""
+    frames_ms = sum(run["profiled_ms"])
+    return {"frames_ms": round(frames_ms, 2), "kernel_ms_sum": round(run["kernel_ms_sum"], 2),
+            "idle_fraction": round(1.0 - run["kernel_ms_sum"] / frames_ms, 4) if frames_ms else None,
+            "frames": run["profiled_frames"]}
 
 
 def run_ours(args) -> None:
@@ -355,12 +512,13 @@ def run_ours(args) -> None:
     scene = scenes.body_scene(frames=args.warmup + args.steps + 1)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     modes = {"plain": kn.MODE_PLAIN_FP64, "mixed": kn.MODE_MIXED}
-    main = time_frames(lib, scene, modes[args.mode], args, torch, flush, world)
+    profile_frames = min(args.steps, args.profile_frames)
+    main = time_frames(lib, scene, modes[args.mode], args, torch, flush, world, profile_frames)
     agg = _aggregate(main, world)
     device_s, value = agg["max_seconds"], agg["value"]
     plain = None
     if args.mode == "mixed" and not args.skip_plain:
-        ref = time_frames(lib, scene, kn.MODE_PLAIN_FP64, args, torch, flush, world)
+        ref = time_frames(lib, scene, kn.MODE_PLAIN_FP64, args, torch, flush, world, min(profile_frames, 2))
         ragg = _aggregate(ref, world)
         plain_s = ragg["max_seconds"]
         plain = {"value": ragg["value"], "unit": UNIT, "ms_per_step": 1e3 * plain_s / args.steps,
@@ -373,9 +531,25 @@ def run_ours(args) -> None:
     # End to end through the public API with host buffers.
     e2e = run_e2e(lib, scene, args, torch) if not args.skip_e2e else None
     roofline = _roofline(main, fp64_peak.value)
-    cpu = None
+    cpu, sample, reference_gpu = None, None, None
+    first = args.warmup + 1
     if rank == 0 and world == 1 and not args.skip_cpu:
-        cpu = cpu_oracle_sample(scenes.body_scene(frames=args.warmup + 3), args.warmup + 1, 1, args.cpu_substeps)
+        # Baseline legs, all from the checkpoint of the timed region's start:
+        # the CPU oracle and both GB300 forms on the same substeps (rate and
+        # deviation), and the reference's own CUDA backend on whole frames.
+        ck = main["start_checkpoint"]
+        cpu = oracle_sample_from(scene, ck, first, args.cpu_substeps, args.cpu_repeats)
+        oq = cpu.pop("q")
+        sample = {"frame": first, "substeps": args.cpu_substeps, "oracle_substeps_per_s": cpu["value"]}
+        for label, mode in (("mixed", kn.MODE_MIXED), ("plain_fp64", kn.MODE_PLAIN_FP64)):
+            g = gpu_sample_from(lib, scene, ck, first, args.cpu_substeps, mode)
+            dq = np.abs(g.pop("q") - oq)
+            g["max_position_dev_m"] = float(dq[:, :3].max())
+            g["max_rotation_dev_rad"] = float(dq[:, 3:].max())
+            sample[label] = g
+        if not args.skip_reference_gpu:
+            reference_gpu = reference_gpu_frames(scene, ck, first, min(args.steps, args.reference_frames),
+                                                 main["frame_ms"], main["frame_substeps"])
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -383,10 +557,14 @@ def run_ours(args) -> None:
             "vs_baseline": None, "dtype": "f64" if args.mode == "plain" else "f64+f32",
             "data": "synthetic (seeded body scene, see kami-hair-solver_gb300/scenes.py)",
             "config": _config(scene, args.mode), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "plain_fp64": plain, "clocks": main["clocks"], "gpu_launches": int(main["launches"]),
+            "plain_fp64": plain, "same_sample": sample, "reference_gpu": reference_gpu,
+            "max_position_dev_m": sample["mixed"]["max_position_dev_m"] if sample else None,
+            "max_rotation_dev_rad": sample["mixed"]["max_rotation_dev_rad"] if sample else None,
+            "host_gap": _host_gap(main), "clocks": main["clocks"], "gpu_launches": int(main["launches"]),
             "wall_s": main["wall_s"], "substeps": main["substeps"], "newton_iterations": main["newton"],
-            "frame_ms": [round(x, 2) for x in main["frame_ms"]], "fp64_pipe_peak_tflops": fp64_peak.value,
-            "fp32_pipe_peak_tflops": fp32_peak.value, "replica_checksums": agg["checksums"],
+            "frame_ms": [round(x, 2) for x in main["frame_ms"]], "frame_substeps": main["frame_substeps"],
+            "fp64_pipe_peak_tflops": fp64_peak.value, "fp32_pipe_peak_tflops": fp32_peak.value,
+            "replica_checksums": agg["checksums"],
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -449,8 +627,15 @@ def main() -> None:
     ap.add_argument("--skip-plain", action="store_true", help="do not time the plain FP64 form beside the mixed one")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--cpu-substeps", type=int, default=2,
+    ap.add_argument("--cpu-substeps", type=int, default=1,
                     help="substeps per sampled frame in the CPU oracle legs")
+    ap.add_argument("--cpu-repeats", type=int, default=3,
+                    help="timed repeats of the CPU oracle sample (each from the same checkpoint)")
+    ap.add_argument("--profile-frames", type=int, default=4,
+                    help="timed frames re-run untimed with per-kernel timing for the kernel shares")
+    ap.add_argument("--reference-frames", type=int, default=3,
+                    help="frames of the reference's own CUDA backend timed beside ours")
+    ap.add_argument("--skip-reference-gpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

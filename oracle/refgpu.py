@@ -1,4 +1,5 @@
-"""The reference's own FP64 CUDA backend, driven from the tests.
+"""ORACLE — test infrastructure only: the reference's own FP64 CUDA backend,
+driven from the tests and from the bench's baseline legs.
 
 ``oracle/_ref/libkhs_ref.so`` is the reference's ``src/cuda_backend.cu``
 compiled unchanged for sm_103a plus ``oracle/ref_bridge.cpp`` (a flat C API
@@ -155,6 +156,12 @@ class RefSolver:
         st.struct_size = ctypes.sizeof(st)
         self._check(self.ref.lib.khsRefStats(self.handle, ctypes.byref(st)))
         return st
+
+    def gpu_stats(self) -> kn.GpuStats:
+        g = kn.GpuStats()
+        g.struct_size = ctypes.sizeof(g)
+        self._check(self.ref.lib.khsRefGpuStats(self.handle, ctypes.byref(g)))
+        return g
 
     def failure(self) -> kn.FailureDiagnostics:
         d = kn.FailureDiagnostics()

@@ -20,6 +20,9 @@ if str(PACKAGE) not in sys.path:
     sys.path.insert(0, str(PACKAGE))
 if str(REPO / "tests") not in sys.path:
     sys.path.insert(0, str(REPO / "tests"))
+# oracle/refgpu.py: the binding of the reference's own CUDA backend.
+if str(REPO / "oracle") not in sys.path:
+    sys.path.append(str(REPO / "oracle"))
 
 ORACLE_SO = REPO / "oracle" / "_build" / "libkhs_oracle.so"
 

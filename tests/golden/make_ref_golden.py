@@ -29,7 +29,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-sys.path[:0] = [str(REPO / "kami-hair-solver_gb300"), str(REPO / "tests")]
+sys.path[:0] = [str(REPO / "kami-hair-solver_gb300"), str(REPO / "tests"), str(REPO / "oracle")]
 
 import khs_native as kn  # noqa: E402
 import refgpu  # noqa: E402

@@ -3,8 +3,7 @@ public header (include/kami_hair_solver.h, ABI v5): every typedef'd struct
 with its field types, names and array lengths, every enum with its member
 values, and every exported function with its normalised signature.
 
-Run in a checkout that has the reference next to it:
-    python tests/golden/make_reference_abi.py /root/reference/include/kami_hair_solver.h
+    python tests/golden/make_reference_abi.py <reference checkout>/include/kami_hair_solver.h
 """
 import json
 import sys
@@ -16,7 +15,9 @@ from abi_parse import parse_header  # noqa: E402
 
 
 def main() -> None:
-    src = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/include/kami_hair_solver.h")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_reference_abi.py <path of the reference's include/kami_hair_solver.h>")
+    src = Path(sys.argv[1])
     abi = parse_header(src.read_text(encoding="utf-8"))
     abi["source"] = "reference include/kami_hair_solver.h (ABI version 5)"
     (HERE / "reference_abi.json").write_text(json.dumps(abi, indent=1, sort_keys=True) + "\n")

@@ -7,15 +7,18 @@ import khs_native as kn
 import scenes
 
 
-def run(lib, scene, frames=None, mode=None, probe=None):
+def run(lib, scene, frames=None, mode=None, probe=None, substep_limit=0):
     """Steps ``scene``; per frame returns result, stats, state and the
     contact records of the last gradient evaluation.  ``probe`` is an
     optional second library whose solver is stepped in lockstep only to
-    classify contacts at this run's own state (bit-exact integer check)."""
+    classify contacts at this run's own state (bit-exact integer check).
+    ``substep_limit`` > 0 ends every frame after that many substeps."""
     s = kn.HairSolver(lib)
     scenes.load_into(s, scene, frames=frames)
     if mode is not None:
         s.set_solve_mode(mode)
+    if substep_limit:
+        s.set_substep_limit(substep_limit)
     p = None
     if probe is not None:
         p = kn.HairSolver(probe)

@@ -74,6 +74,32 @@ def checkpoint(frame: int, q: np.ndarray, v: np.ndarray) -> bytes:
         np.ascontiguousarray(q, dtype=np.float64).tobytes() + np.ascontiguousarray(v, dtype=np.float64).tobytes()
 
 
+def sensitivity(oracle_lib, case: str, frames: int | None = None) -> list[tuple[float, float]]:
+    """Per frame, how far the oracle's own trajectory moves (positions,
+    rotations) when the root targets change by +-1e-15 relative: the
+    amplification of last-bit differences that belongs to the scene."""
+    import parity
+
+    base = parity.run(oracle_lib, SCENES[case](), frames=frames)
+    out = [(0.0, 0.0)] * len(base)
+    for eps in (1e-15, -1e-15):
+        sc = SCENES[case]()
+        pts = sc.root_points_at
+        sc.root_points_at = lambda f, pts=pts, eps=eps: pts(f) * (1.0 + eps)
+        for k, fr in enumerate(parity.compare(parity.run(oracle_lib, sc, frames=frames), base)):
+            out[k] = (max(out[k][0], fr["max_position"]), max(out[k][1], fr["max_rotation"]))
+    return out
+
+
+def tolerances(g: dict, case: str, sens: list[tuple[float, float]]) -> list[tuple[float, float]]:
+    """Per frame (position, rotation) tolerance against the reference:
+    1e-6 m / 1e-6 rad, or 4x the larger of the reference's run-to-run
+    spread and the oracle's sensitivity where that is larger."""
+    spread = g[f"{case}__spread"]
+    return [(max(TOL, 4.0 * max(spread[k, 0], s[0])), max(TOL, 4.0 * max(spread[k, 1], s[1])))
+            for k, s in enumerate(sens)]
+
+
 def trajectory_deviation(g: dict, case: str, frames: list[dict]) -> list[dict]:
     """Per stepped frame: max position / rotation deviation from the
     reference's run, and each library-vs-reference count pair."""
@@ -91,10 +117,28 @@ def trajectory_deviation(g: dict, case: str, frames: list[dict]) -> list[dict]:
     return out
 
 
-def step_from_reference_state(lib, g: dict, case: str, frame: int, mode: int | None = None) -> dict:
+def frame_tolerance(oracle_lib, g: dict, case: str, frame: int) -> tuple[float, float]:
+    """(position, rotation) tolerance of one frame from the reference's
+    state: 1e-6, or 4x the oracle's change under a +-1e-15 relative change
+    of the root targets over that frame where that is larger."""
+    base = step_from_reference_state(oracle_lib, g, case, frame, q_out=True)["q"]
+    pos = rot = 0.0
+    for eps in (1e-15, -1e-15):
+        q = step_from_reference_state(oracle_lib, g, case, frame, eps=eps, q_out=True)["q"]
+        dq = np.abs(q - base)
+        pos, rot = max(pos, float(dq[:, :3].max())), max(rot, float(dq[:, 3:].max()))
+    return max(TOL, 4.0 * pos), max(TOL, 4.0 * rot)
+
+
+def step_from_reference_state(lib, g: dict, case: str, frame: int, mode: int | None = None, eps: float = 0.0,
+                              q_out: bool = False) -> dict:
     """Restores the reference's state after ``frame`` (full q, v from the
-    fixture) into ``lib`` and steps frame ``frame + 1``."""
+    fixture) into ``lib`` and steps frame ``frame + 1`` (root targets scaled
+    by 1 + ``eps``)."""
     sc = SCENES[case]()
+    if eps:
+        pts = sc.root_points_at
+        sc.root_points_at = lambda f: pts(f) * (1.0 + eps)
     s = kn.HairSolver(lib)
     scenes.load_into(s, sc)
     if mode is not None:
@@ -106,5 +150,6 @@ def step_from_reference_state(lib, g: dict, case: str, frame: int, mode: int | N
     s.close()
     dq = np.abs(q - g[f"{case}__q"][frame])
     return {"result": r, "position": float(dq[:, :3].max()), "rotation": float(dq[:, 3:].max()),
+            "q": q if q_out else None,
             "counts": {c: (int(getattr(st, c)), int(stat(g, case, frame, c)), int(stat(g, case, frame, c, "stats_b")))
                        for c in COUNTS}}

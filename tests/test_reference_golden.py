@@ -27,10 +27,11 @@ def golden():
 def test_oracle_follows_reference_trajectory(oracle_lib, golden, case):
     frames = parity.run(oracle_lib, rg.SCENES[case]())
     report = rg.trajectory_deviation(golden, case, frames)
+    tol = rg.tolerances(golden, case, rg.sensitivity(oracle_lib, case))
     assert len(report) == len(golden[f"{case}__result"])
-    for fr in report:
+    for k, fr in enumerate(report):
         assert fr["result"] == (0, 0), fr
-        assert fr["position"] <= rg.TOL and fr["rotation"] <= rg.TOL, fr
+        assert fr["position"] <= tol[k][0] and fr["rotation"] <= tol[k][1], (fr, tol[k])
         for c in rg.COUNTS:
             assert rg.count_ok(*fr[c]), (c, fr)
 
@@ -38,8 +39,9 @@ def test_oracle_follows_reference_trajectory(oracle_lib, golden, case):
 @pytest.mark.parametrize("case,frame", [("pole", 1), ("sphere_moving", 1), ("sphere_moving", 2), ("ellipsoid40", 1)])
 def test_oracle_one_frame_from_reference_state(oracle_lib, golden, case, frame):
     out = rg.step_from_reference_state(oracle_lib, golden, case, frame)
+    tol = rg.frame_tolerance(oracle_lib, golden, case, frame)
     assert out["result"] == 0
-    assert out["position"] <= rg.TOL and out["rotation"] <= rg.TOL, out
+    assert out["position"] <= tol[0] and out["rotation"] <= tol[1], (out, tol)
     for c, (ours, a, b) in out["counts"].items():
         assert rg.count_ok(ours, a, b), (c, out)
 
