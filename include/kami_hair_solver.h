@@ -410,9 +410,12 @@ KHS_API uint32_t khsxGetSolveMode(const KhsSolver *solver);
    once per solver by timing each shape on the first system; this pins it:
    strands_per_warp 5 (6 lanes per strand), 2 (12 lanes per strand, half
    the instructions on each strand's sequential chain) or 1 (18 lanes),
-   blocks_per_sm 1-8; long_strands > 0 (with strands_per_warp 5) first gives
-   that many longest strands one warp of 18 lanes each.  strands_per_warp 0
-   restores the tuning.  Every shape gives bit-identical directions.
+   blocks_per_sm 1-8; long_strands > 0 first gives that many longest
+   strands one warp of 18 lanes each (with strands_per_warp 5) or a pair of
+   warps each (with strands_per_warp 1: one warp runs the pivot steps on the
+   diagonal blocks, the other applies them to the coupling blocks and the
+   right-hand side), the rest five per warp.  strands_per_warp 0 restores
+   the tuning.  Every shape gives bit-identical directions.
    Requires a built solver. */
 KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *solver, uint32_t strands_per_warp, uint32_t blocks_per_sm,
                                             uint32_t long_strands);

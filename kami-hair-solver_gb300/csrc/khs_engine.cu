@@ -1806,6 +1806,269 @@ __global__ void __launch_bounds__(128) k_block_solve_hybrid(View d, uint32_t lon
     }
 }
 
+// ---- long strands on a pair of warps ------------------------------------
+//
+// On GB300 one FP64 warp instruction holds a sub-partition's FP64 pipe for
+// about 64 cycles whatever the number of active lanes, so a strand solved by
+// one warp is bound by the FP64 instructions of its per-node chain (about 110
+// per node with 18 lanes).  Here the longest strands are solved by two warps
+// of one block, which the SM places on two sub-partitions:
+// * the B warp holds the Schur complement B_n (lane (r, h): row r, columns
+//   2h, 2h+1), adds the relative shift and runs the six pivot steps --
+//   pivot search, row swap, pivot reciprocal, row factors, update of the
+//   remaining columns -- and publishes each step's pivot row, reciprocal
+//   and row factors in shared memory;
+// * the U warp holds [U_n | rhs_n] in the same lane layout, applies each
+//   published step to it one step behind, scales the rows, stores C_n and
+//   d'_n, and forms the next Schur complement B_{n+1} = D_{n+1} - U_n^T C_n
+//   and right-hand side, which it hands to the B warp; it also runs the back
+//   substitution.
+// Every entry goes through the same operations in the same order as in
+// solve_group_aug<3>, so the directions are identical bit for bit.  The two
+// warps meet at a named barrier (bar.sync, 64 threads) once per pivot step
+// and once per node; both execute the same number of barriers by
+// construction (same strand length, six steps per node, no early exit).
+struct PairShared {
+    double B[36];      // B_n, row-major, from the U warp to the B warp
+    double fp[2][6];   // row factors a[r][col] * (1 / pivot) of a step (double-buffered by step parity)
+    double ip[2];      // the step's pivot reciprocal
+    int pivot[2];      // the step's pivot row
+    int ok[2];         // no pivot failure in this node up to and including the step
+    uint32_t item;     // work item, from the B warp to the U warp
+};
+
+__device__ __forceinline__ void pair_barrier(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+
+__device__ __forceinline__ void pair_strand_range(const View &d, uint32_t k, uint32_t &begin, uint32_t &len)
+{
+    const uint32_t s = d.sorder[k];
+    begin = d.sfirst[s] + d.sfixed[s];
+    const uint32_t end = d.sfirst[s] + d.scount[s];
+    len = end > begin ? end - begin : 0;
+}
+
+// B warp of a pair (see above): pivot steps on the Schur complements.
+__device__ void solve_pair_b(const View &d, uint32_t k, PairShared &sh, int bar)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gl = lane < 18 ? lane : lane - 18;  // lanes 18-31 shadow lanes 0-13 and write nothing
+    const int r = gl % 6, h = gl / 6, c0 = 2 * h;
+    uint32_t begin, len;
+    pair_strand_range(d, k, begin, len);
+    for (uint32_t t = 0; t < len; ++t) {
+        pair_barrier(bar);  // B_t is in shared memory
+        double a[2] = {sh.B[6 * r + c0], sh.B[6 * r + c0 + 1]};
+        double diag_r = 0.0;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) if (c0 + j == r) diag_r = a[j];
+        unsigned long long smax = 0ull;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(__shfl_sync(FULL, diag_r, 6 * (q / 2) + q)) &
+                                         0x7fffffffffffffffull;
+            smax = b > smax ? b : smax;
+        }
+        const double shift = fmax(__dmul_rn(1.0e-12, __longlong_as_double((long long)smax)), 1.0e-24);
+#pragma unroll
+        for (int j = 0; j < 2; ++j) if (c0 + j == r) a[j] = __dadd_rn(a[j], shift);
+        bool ok = true;
+#pragma unroll
+        for (int col = 0; col < 6; ++col) {
+            const int hc = col / 2, jc = col % 2, owner_half = 6 * hc;
+            double acol = 0.0;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) if (j == jc && h == hc) acol = a[j];
+            const unsigned long long mb = (unsigned long long)__double_as_longlong(acol) & 0x7fffffffffffffffull;
+            int pivot = col;
+            unsigned long long best = __shfl_sync(FULL, mb, owner_half + col);
+#pragma unroll
+            for (int row = col + 1; row < 6; ++row) {
+                const unsigned long long vrow = __shfl_sync(FULL, mb, owner_half + row);
+                if (vrow > best) { best = vrow; pivot = row; }
+            }
+            if (best < 0x39b4484bfeebc2a0ull || best >= 0x7ff0000000000000ull) ok = false;
+            const int partner = r == col ? pivot : (r == pivot ? col : r);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) a[j] = __shfl_sync(FULL, a[j], 6 * h + partner);
+            acol = 0.0;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) if (j == jc && h == hc) acol = a[j];
+            const double ip = __drcp_rn(__shfl_sync(FULL, acol, owner_half + col));
+            const double fp = __dmul_rn(__shfl_sync(FULL, acol, owner_half + r), ip);
+            const int prow = 6 * h + col;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                if (2 * 2 + j <= col) continue;  // finished in every lane
+                const double x = __shfl_sync(FULL, a[j], prow);
+                a[j] = (r == col) ? a[j] : __fma_rn(-fp, x, a[j]);
+            }
+            const int slot = col & 1;
+            if (lane < 6) sh.fp[slot][lane] = fp;
+            if (lane == 0) {
+                sh.ip[slot] = ip;
+                sh.pivot[slot] = pivot;
+                sh.ok[slot] = ok ? 1 : 0;
+            }
+            pair_barrier(bar);  // step published
+        }
+    }
+}
+
+// U warp of a pair (see above): the published steps applied to [U_n | rhs_n],
+// the next Schur complement, and the back substitution.
+__device__ void solve_pair_u(const View &d, uint32_t k, PairShared &sh, int bar)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gl = lane < 18 ? lane : lane - 18;
+    const int r = gl % 6, h = gl / 6, c0 = 2 * h;
+    const bool writer = lane < 18;
+    uint32_t begin, len;
+    pair_strand_range(d, k, begin, len);
+    double nd[2], nu[2], nuc[6], ng = 0.0;
+    auto fetch = [&](uint32_t t) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) nd[j] = on ? d.diag[36 * n + 6 * r + c0 + j] : 0.0;
+        ng = on ? d.grad[6 * n + r] : 0.0;
+        const bool up = on && t + 1 < len;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) nu[j] = up ? d.upper[36 * n + 6 * r + c0 + j] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) nuc[q] = (on && t > 0) ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
+    };
+    fetch(0);
+    double Cprev[2] = {0.0, 0.0}, dprev = 0.0;
+    bool failed = false;
+    for (uint32_t t = 0; t < len; ++t) {
+        const bool on = !failed;
+        const size_t n = begin + t;
+        double a[2] = {nd[0], nd[1]}, u[2] = {nu[0], nu[1]}, ucol[6], rhs = -ng;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) ucol[q] = nuc[q];
+        if (t + 1 < len) fetch(t + 1);
+        if (t > 0) {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+#pragma unroll
+                for (int j = 0; j < 2; ++j) a[j] = __fma_rn(-ucol[q], __shfl_sync(FULL, Cprev[j], 6 * h + q), a[j]);
+                rhs = __fma_rn(-ucol[q], __shfl_sync(FULL, dprev, q), rhs);
+            }
+        }
+        if (writer) {
+            sh.B[6 * r + c0] = a[0];
+            sh.B[6 * r + c0 + 1] = a[1];
+        }
+        pair_barrier(bar);  // hand B_t over
+        double ipiv = 1.0;
+        bool ok = true;
+#pragma unroll
+        for (int col = 0; col < 6; ++col) {
+            pair_barrier(bar);  // step published
+            const int slot = col & 1;
+            const int pivot = sh.pivot[slot];
+            const double fp = sh.fp[slot][r], ip = sh.ip[slot];
+            ok = sh.ok[slot] != 0;
+            const int partner = r == col ? pivot : (r == pivot ? col : r);
+            const int src = 6 * h + partner;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) u[j] = __shfl_sync(FULL, u[j], src);
+            rhs = __shfl_sync(FULL, rhs, src);
+            if (r == col) ipiv = ip;
+            const int prow = 6 * h + col;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const double x = __shfl_sync(FULL, u[j], prow);
+                u[j] = (r == col) ? u[j] : __fma_rn(-fp, x, u[j]);
+            }
+            const double xr = __shfl_sync(FULL, rhs, prow);
+            rhs = (r == col) ? rhs : __fma_rn(-fp, xr, rhs);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) u[j] = __dmul_rn(u[j], ipiv);
+        rhs = __dmul_rn(rhs, ipiv);
+        if (on && !ok) {
+            failed = true;
+            if (lane == 0) atomicExch(&d.sc->solve_failed, 1);
+        }
+        Cprev[0] = u[0];
+        Cprev[1] = u[1];
+        dprev = rhs;
+        if (on && !failed && writer) {
+#pragma unroll
+            for (int j = 0; j < 2; ++j) d.cprime[36 * n + 6 * r + c0 + j] = u[j];
+            if (h == 0) d.dprime[6 * n + r] = rhs;
+        }
+    }
+    __syncwarp();  // C_n and d'_n written by the other lanes of this warp
+    double next = 0.0, pc[6], pd = 0.0;
+    auto fetch_back = [&](uint32_t t) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        pd = on ? d.dprime[6 * n + r] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) pc[q] = on ? d.cprime[36 * n + 6 * r + q] : 0.0;
+    };
+    if (len) fetch_back(len - 1);
+    for (uint32_t t = len; t-- > 0;) {
+        const bool on = !failed;
+        const size_t n = begin + t;
+        double value = pd, crow[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) crow[q] = pc[q];
+        if (t > 0) fetch_back(t - 1);
+        const bool coupled = on && t + 1 < len;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const double dq = __shfl_sync(FULL, next, q);
+            if (coupled) value = __fma_rn(-crow[q], dq, value);
+        }
+        if (on && h == 0 && writer) d.dir[6 * n + r] = value;
+        next = on ? value : 0.0;
+    }
+}
+
+// Pair schedule: the `long_strands` longest strands each on a pair of
+// warps (solve_pair_b / solve_pair_u), then the rest five per warp.  Blocks
+// of four warps hold two pairs.  A pair takes work items together while
+// they are long strands; at the first item past them both warps go on alone
+// through the five-strand groups.
+__global__ void __launch_bounds__(128) k_block_solve_pairs(View d, uint32_t long_strands)
+{
+    __shared__ PairShared shared[2];
+    const int warp = threadIdx.x >> 5, pair = warp >> 1, role = warp & 1;
+    const int bar = 1 + pair;
+    PairShared &sh = shared[pair];
+    const uint32_t rest = d.S > long_strands ? d.S - long_strands : 0;
+    const uint32_t items = long_strands + (rest + AugLayout<1>::kStrands - 1) / AugLayout<1>::kStrands;
+    bool paired = true;
+    for (;;) {
+        uint32_t g = 0;
+        if (paired) {
+            if (role == 0 && (threadIdx.x & 31) == 0) sh.item = atomicAdd(&d.sc->solve_next, 1u);
+            pair_barrier(bar);
+            g = sh.item;
+            if (g < long_strands) {
+                if (role == 0) solve_pair_b(d, g, sh, bar);
+                else solve_pair_u(d, g, sh, bar);
+                continue;
+            }
+            paired = false;  // every later item is a five-strand group
+            if (role == 1) {
+                if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+                g = __shfl_sync(0xffffffffu, g, 0);
+            }
+        } else {
+            if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+            g = __shfl_sync(0xffffffffu, g, 0);
+        }
+        if (g >= items) break;
+        solve_group_aug<1>(d, g - long_strands, long_strands);
+    }
+}
+
 template<int H> __global__ void __launch_bounds__(128) k_block_solve_aug(View d)
 {
     const uint32_t groups = (d.S + AugLayout<H>::kStrands - 1) / AugLayout<H>::kStrands;
@@ -2658,7 +2921,8 @@ struct Engine::Impl {
         out_next = 0;
     }
     void (*solve_kernel)(View) = nullptr;
-    uint32_t solve_long = 0;  // > 0: k_block_solve_hybrid with this many long strands
+    uint32_t solve_long = 0;  // > 0: k_block_solve_hybrid / k_block_solve_pairs with this many long strands
+    bool solve_pairs = false; // the long strands on warp pairs (k_block_solve_pairs)
     std::vector<uint32_t> sorted_len;  // free nodes per strand, in the solve order
     unsigned ff_blocks = 0;     // launch shape of the float-float kernels
     std::vector<KernelStat> kstats;
@@ -3203,9 +3467,12 @@ bool Engine::make_steepest()
 KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm, uint32_t long_strands)
 {
     Impl &I = *d_;
-    if (strands_per_warp == 0) { I.solve_blocks = 0; I.solve_kernel = nullptr; I.solve_long = 0; return KHS_OK; }
+    if (strands_per_warp == 0) {
+        I.solve_blocks = 0; I.solve_kernel = nullptr; I.solve_long = 0; I.solve_pairs = false;
+        return KHS_OK;
+    }
     if ((strands_per_warp != 5 && strands_per_warp != 2 && strands_per_warp != 1) || blocks_per_sm < 1 || blocks_per_sm > 8 ||
-        (long_strands && (strands_per_warp != 5 || long_strands >= I.v.S)))
+        (long_strands && ((strands_per_warp != 5 && strands_per_warp != 1) || long_strands >= I.v.S)))
         return KHS_ERROR_INVALID_ARGUMENT;
     int sms = 0;
     KHS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, kDevice));
@@ -3216,6 +3483,7 @@ KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t b
                      : strands_per_warp == 2 ? k_block_solve_aug<2>
                                              : k_block_solve_aug<3>;
     I.solve_long = long_strands;
+    I.solve_pairs = long_strands && strands_per_warp == 1;
     I.solve_blocks = std::min(std::max(1u, (groups + 3) / 4), blocks_per_sm * unsigned(sms));
     const unsigned ff_groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
     I.ff_blocks = std::min(std::max(1u, (ff_groups + 3) / 4), 2u * unsigned(sms));
@@ -3230,12 +3498,13 @@ void Engine::tune_block_solve()
     cudaEvent_t ev[2];
     KHS_CUDA(cudaEventCreate(&ev[0]));
     KHS_CUDA(cudaEventCreate(&ev[1]));
-    auto time_it = [&](void (*kernel)(View), unsigned blocks, uint32_t nlong) {
+    auto time_it = [&](void (*kernel)(View), unsigned blocks, uint32_t nlong, bool pairs = false) {
         float best = 3.0e38f;
         for (int rep = 0; rep < 2; ++rep) {
             KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
             KHS_CUDA(cudaEventRecord(ev[0], I.stream));
             if (kernel) kernel<<<blocks, 128, 0, I.stream>>>(I.v);
+            else if (pairs) k_block_solve_pairs<<<blocks, 128, 0, I.stream>>>(I.v, nlong);
             else k_block_solve_hybrid<<<blocks, 128, 0, I.stream>>>(I.v, nlong);
             ++I.launches;
             KHS_CUDA(cudaEventRecord(ev[1], I.stream));
@@ -3255,12 +3524,14 @@ void Engine::tune_block_solve()
         for (unsigned per_sm = 1; per_sm <= 4; ++per_sm) {
             const unsigned blocks = std::min(most, per_sm * unsigned(sms));
             const float ms = time_it(c.kernel, blocks, 0);
-            if (ms < best_ms) { best_ms = ms; I.solve_kernel = c.kernel; I.solve_blocks = blocks; I.solve_long = 0; }
+            if (ms < best_ms) {
+                best_ms = ms; I.solve_kernel = c.kernel; I.solve_blocks = blocks; I.solve_long = 0; I.solve_pairs = false;
+            }
             if (blocks == most) break;
         }
     }
     // Hybrid: the strands of at least `cut` free nodes one per warp (18
-    // lanes), the rest five per warp.
+    // lanes) or on a pair of warps, the rest five per warp.
     uint32_t last_long = 0;
     for (uint32_t cut : {160u, 128u, 96u, 64u, 48u}) {
         const uint32_t nlong = uint32_t(std::count_if(I.sorted_len.begin(), I.sorted_len.end(),
@@ -3271,8 +3542,12 @@ void Engine::tune_block_solve()
         const unsigned most = std::max(1u, (groups + 3) / 4);
         for (unsigned per_sm = 1; per_sm <= 3; ++per_sm) {
             const unsigned blocks = std::min(most, per_sm * unsigned(sms));
-            const float ms = time_it(nullptr, blocks, nlong);
-            if (ms < best_ms) { best_ms = ms; I.solve_kernel = nullptr; I.solve_blocks = blocks; I.solve_long = nlong; }
+            for (bool pairs : {false, true}) {
+                const float ms = time_it(nullptr, blocks, nlong, pairs);
+                if (ms < best_ms) {
+                    best_ms = ms; I.solve_kernel = nullptr; I.solve_blocks = blocks; I.solve_long = nlong; I.solve_pairs = pairs;
+                }
+            }
             if (blocks == most) break;
         }
     }
@@ -3291,6 +3566,7 @@ void Engine::launch_block_solve()
 {
     Impl &I = *d_;
     if (I.solve_kernel) I.launch("k_block_solve", I.solve_kernel, I.solve_blocks, 128, I.v);
+    else if (I.solve_pairs) I.launch("k_block_solve", k_block_solve_pairs, I.solve_blocks, 128, I.v, I.solve_long);
     else I.launch("k_block_solve", k_block_solve_hybrid, I.solve_blocks, 128, I.v, I.solve_long);
 }
 

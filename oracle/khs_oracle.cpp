@@ -69,6 +69,108 @@ constexpr uint32_t kNone = 0xffffffffu;
 static uint32_t g_substep_limit = 0;
 
 // ---------------------------------------------------------------------------
+// Strand partition (the sharded-solve design, on CPU ranks).
+//
+// Strands are independent in assembly, factorisation and contact; the solve
+// couples them only through global scalars: energies, the gradient norm, the
+// slope g.d, the direction norm, the CCD step bound, the largest node
+// translation, the candidate and active-contact counts, feasibility and
+// failure flags.  A partitioned solver works on strands [s0, s1) only and
+// combines those scalars with a caller-supplied all-reduce over int64
+// arrays.  Sums are exact (ExactSum: a fixed-point accumulator whose limbs
+// add as integers, rounded once to the nearest double), so the result does
+// not depend on how the strands are split: N ranks give the bits of one.
+
+// all-reduce in place over `count` int64 values; op 0 = sum, 1 = min, 2 = max.
+using ReduceFn = void (*)(void *ctx, int64_t *values, uint32_t count, int op);
+
+struct ExactSum {
+    static constexpr int kLimbs = 68;     // 32-bit limbs from 2^-1088 up: every finite double fits
+    static constexpr int kBase = -1088;
+    static constexpr int kSize = kLimbs + 3;  // + counts of NaN, +inf, -inf terms
+    int64_t v[kSize] = {};
+
+    void add(double x)
+    {
+        if (std::isnan(x)) { ++v[kLimbs]; return; }
+        if (std::isinf(x)) { ++v[x > 0 ? kLimbs + 1 : kLimbs + 2]; return; }
+        if (x == 0.0) return;
+        int e = 0;
+        const double m = std::frexp(std::fabs(x), &e);   // |x| = m 2^e, m in [0.5, 1)
+        uint64_t M = uint64_t(std::ldexp(m, 53));         // |x| = M 2^(e - 53), exactly
+        int lo = e - 53;
+        if (lo < -1074) { M >>= (-1074 - lo); lo = -1074; }  // subnormal: exact multiple of 2^-1074
+        const int p = lo - kBase, i = p / 32, o = p % 32;
+        const unsigned __int128 w = (unsigned __int128)M << o;
+        const int64_t s = x < 0 ? -1 : 1;
+        v[i] += s * int64_t(uint64_t(w) & 0xffffffffull);
+        v[i + 1] += s * int64_t(uint64_t(w >> 32) & 0xffffffffull);
+        v[i + 2] += s * int64_t(uint64_t(w >> 64));
+    }
+
+    // The exact sum rounded to the nearest double (ties to even).
+    double value() const
+    {
+        if (v[kLimbs] || (v[kLimbs + 1] && v[kLimbs + 2])) return std::numeric_limits<double>::quiet_NaN();
+        if (v[kLimbs + 1]) return std::numeric_limits<double>::infinity();
+        if (v[kLimbs + 2]) return -std::numeric_limits<double>::infinity();
+        int64_t a[kLimbs];
+        std::copy(v, v + kLimbs, a);
+        auto normalise = [&]() {
+            for (int i = 0; i + 1 < kLimbs; ++i) {
+                const int64_t c = a[i] >> 32;  // floor division by 2^32
+                a[i] -= c * (int64_t(1) << 32);
+                a[i + 1] += c;
+            }
+        };
+        normalise();
+        const bool neg = a[kLimbs - 1] < 0;
+        if (neg) {
+            for (int64_t &x : a) x = -x;
+            normalise();
+        }
+        int t = kLimbs - 1;
+        while (t >= 0 && a[t] == 0) --t;
+        if (t < 0) return 0.0;
+        auto limb = [&](int i) { return i >= 0 ? uint64_t(a[i]) : 0ull; };
+        const unsigned __int128 X = ((unsigned __int128)limb(t) << 64) | ((unsigned __int128)limb(t - 1) << 32) | limb(t - 2);
+        bool sticky = false;
+        for (int i = 0; i < t - 2; ++i) sticky = sticky || a[i] != 0;
+        const int lsb = 32 * (t - 2) + kBase;  // exponent of X's lowest bit
+        int L = 127;
+        while (!((X >> L) & 1)) --L;
+        const int keep = std::max(L + lsb - 52, -1074);  // exponent of the lowest kept bit
+        const int sh = keep - lsb;
+        unsigned __int128 mant;
+        if (sh <= 0) {
+            mant = X << (-sh);
+        } else {
+            mant = X >> sh;
+            const unsigned __int128 rem = X & ((((unsigned __int128)1) << sh) - 1);
+            const unsigned __int128 half = ((unsigned __int128)1) << (sh - 1);
+            if (rem > half || (rem == half && (sticky || (mant & 1)))) ++mant;
+        }
+        const double r = std::ldexp(double(uint64_t(mant)), keep);
+        return neg ? -r : r;
+    }
+};
+
+// Order-preserving int64 key of a double (for min/max all-reduce).
+inline int64_t order_key(double x)
+{
+    int64_t b;
+    std::memcpy(&b, &x, 8);
+    return b >= 0 ? b : b ^ std::numeric_limits<int64_t>::max();
+}
+inline double from_order_key(int64_t k)
+{
+    const int64_t b = k >= 0 ? k : k ^ std::numeric_limits<int64_t>::max();
+    double x;
+    std::memcpy(&x, &b, 8);
+    return x;
+}
+
+// ---------------------------------------------------------------------------
 // Geometry.
 
 struct Pair { double distance, t; V3 bary; };
@@ -886,6 +988,25 @@ public:
         }
     }
     void set_substep_limit(uint32_t n) { substep_limit_ = n; }
+
+    // Strand partition (see ReduceFn): from now on this solver steps only
+    // strands [s0, s1) and combines global quantities with `fn`.  Requires a
+    // built solver.
+    KhsResult set_partition(uint32_t s0, uint32_t s1, ReduceFn fn, void *ctx)
+    {
+        if (!built_ || !fn || s0 >= s1 || s1 > strands_.size()) return KHS_ERROR_INVALID_ARGUMENT;
+        part_ = true;
+        reduce_ = fn;
+        reduce_ctx_ = ctx;
+        s_lo_ = s0; s_hi_ = s1;
+        n_lo_ = strands_[s0].first;
+        n_hi_ = size_t(strands_[s1 - 1].first) + strands_[s1 - 1].count;
+        e_lo_ = 0;
+        while (e_lo_ < E() && elements_[e_lo_].strand < s0) ++e_lo_;
+        e_hi_ = e_lo_;
+        while (e_hi_ < E() && elements_[e_hi_].strand < s1) ++e_hi_;
+        return KHS_OK;
+    }
     uint32_t record_count() const { return uint32_t(records_.size()); }
     KhsResult copy_records(KhsxSubstepRecord *out, uint32_t cap) const
     {
@@ -1349,7 +1470,7 @@ private:
         const KhsHairMaterial &m = material_;
         const double inv = 1.0 / dt, inv2 = inv * inv;
 #pragma omp parallel for schedule(static)
-        for (long long ni = 0; ni < (long long)n; ++ni) {
+        for (long long ni = (long long)nlo(); ni < (long long)nhi(); ++ni) {
             const size_t k = size_t(ni);
             if (grad) for (int z = 0; z < 36; ++z) diag_[36 * k + z] = 0.0;
             if (grad) for (int d = 0; d < 6; ++d) grad_[6 * k + d] = 0.0;
@@ -1371,11 +1492,11 @@ private:
         }
         if (grad) std::fill(upper_.begin(), upper_.end(), 0.0);
 #pragma omp parallel for schedule(dynamic, 64)
-        for (long long ei = 0; ei < (long long)ne; ++ei) eval_element(size_t(ei), grad, eo[size_t(ei)]);
+        for (long long ei = (long long)elo(); ei < (long long)ehi(); ++ei) eval_element(size_t(ei), grad, eo[size_t(ei)]);
         // Ordered scatter: node term, then incident elements by index.
         if (grad) {
 #pragma omp parallel for schedule(static)
-            for (long long ei = 0; ei < (long long)ne; ++ei) {
+            for (long long ei = (long long)elo(); ei < (long long)ehi(); ++ei) {
                 // upper block of node i belongs to element (i, j) only.
                 const Element &e = elements_[size_t(ei)];
                 const ElemOut &o = eo[size_t(ei)];
@@ -1384,7 +1505,7 @@ private:
                     for (int a = 0; a < 3; ++a)
                         for (int b = 0; b < 3; ++b) upper_[36 * e.i + 6 * a + b] += o.chij[3 * a + b];
             }
-            for (size_t ei = 0; ei < ne; ++ei) {
+            for (size_t ei = elo(); ei < ehi(); ++ei) {
                 const Element &e = elements_[ei];
                 const ElemOut &o = eo[ei];
                 for (int d = 0; d < 6; ++d) { grad_[6 * e.i + d] += o.gi[d]; }
@@ -1403,22 +1524,62 @@ private:
         }
         Stats st;
         double node_sum = 0, kin = 0, el = 0, co = 0;
-        for (size_t k = 0; k < n; ++k) { node_sum += node_obj[k]; kin += node_kin[k]; }
-        for (size_t ei = 0; ei < ne; ++ei) {
-            const ElemOut &o = eo[ei];
-            el += o.elastic;
-            st.candidates += o.candidates;
-            if (o.closest != kNone) {
-                st.minimum_gap = std::fmin(st.minimum_gap, o.gap);
-                if (!o.feasible) st.feasible = false;
-                if (o.active) ++st.active;
-                if (o.has_contact_terms) co += o.contact;
+        if (part_) {
+            // Exact sums over this range, combined across the ranks.
+            ExactSum sn, sk, se, sc;
+            for (size_t k = nlo(); k < nhi(); ++k) { sn.add(node_obj[k]); sk.add(node_kin[k]); }
+            int64_t counts[2] = {0, 0};
+            for (size_t ei = elo(); ei < ehi(); ++ei) {
+                const ElemOut &o = eo[ei];
+                se.add(o.elastic);
+                counts[0] += o.candidates;
+                if (o.closest != kNone) {
+                    st.minimum_gap = std::fmin(st.minimum_gap, o.gap);
+                    if (!o.feasible) st.feasible = false;
+                    if (o.active) ++counts[1];
+                    if (o.has_contact_terms) sc.add(o.contact);
+                }
+            }
+            // One sum all-reduce (four exact sums, two counts) and one
+            // min all-reduce (minimum gap, feasibility) per evaluation.
+            constexpr int K = ExactSum::kSize;
+            std::vector<int64_t> sums(4 * K + 2);
+            std::copy(sn.v, sn.v + K, sums.begin());
+            std::copy(sk.v, sk.v + K, sums.begin() + K);
+            std::copy(se.v, se.v + K, sums.begin() + 2 * K);
+            std::copy(sc.v, sc.v + K, sums.begin() + 3 * K);
+            sums[4 * K] = counts[0];
+            sums[4 * K + 1] = counts[1];
+            reduce_(reduce_ctx_, sums.data(), uint32_t(sums.size()), 0);
+            std::copy(sums.begin(), sums.begin() + K, sn.v);
+            std::copy(sums.begin() + K, sums.begin() + 2 * K, sk.v);
+            std::copy(sums.begin() + 2 * K, sums.begin() + 3 * K, se.v);
+            std::copy(sums.begin() + 3 * K, sums.begin() + 4 * K, sc.v);
+            node_sum = sn.value(); kin = sk.value(); el = se.value(); co = sc.value();
+            st.candidates = uint64_t(sums[4 * K]);
+            st.active = uint64_t(sums[4 * K + 1]);
+            int64_t mins[2] = {order_key(st.minimum_gap), st.feasible ? 1 : 0};
+            reduce_(reduce_ctx_, mins, 2, 1);
+            st.minimum_gap = from_order_key(mins[0]);
+            st.feasible = mins[1] != 0;
+        } else {
+            for (size_t k = 0; k < n; ++k) { node_sum += node_obj[k]; kin += node_kin[k]; }
+            for (size_t ei = 0; ei < ne; ++ei) {
+                const ElemOut &o = eo[ei];
+                el += o.elastic;
+                st.candidates += o.candidates;
+                if (o.closest != kNone) {
+                    st.minimum_gap = std::fmin(st.minimum_gap, o.gap);
+                    if (!o.feasible) st.feasible = false;
+                    if (o.active) ++st.active;
+                    if (o.has_contact_terms) co += o.contact;
+                }
             }
         }
         st.objective = (node_sum + el) + co;
         st.kinetic = kin; st.elastic = el; st.contact = co;
         if (grad) {
-            for (size_t ei = 0; ei < ne; ++ei) {
+            for (size_t ei = elo(); ei < ehi(); ++ei) {
                 const ElemOut &o = eo[ei];
                 contact_records_[ei] = KhsxContactRecord{o.candidates, o.closest, o.active ? 1u : 0u, 0u, o.gap};
             }
@@ -1464,7 +1625,7 @@ private:
         std::fill(dir_.begin(), dir_.end(), 0.0);
         std::atomic<int> failed{0};
 #pragma omp parallel for schedule(dynamic, 16)
-        for (long long si = 0; si < (long long)strands_.size(); ++si) {
+        for (long long si = (long long)slo(); si < (long long)shi(); ++si) {
             const Strand st = strands_[size_t(si)];
             const uint32_t begin = st.first + st.fixed_count, end = st.first + st.count;
             if (begin >= end) continue;
@@ -1516,7 +1677,7 @@ private:
                 }
             }
         }
-        return failed.load() == 0;
+        return all_int(failed.load(), 2) == 0;
     }
 
     static double dotv(const std::vector<double> &a, const std::vector<double> &b)
@@ -1526,13 +1687,23 @@ private:
         return s;
     }
     static double nrm2(const std::vector<double> &a) { return std::sqrt(dotv(a, a)); }
+    // Global dot product / norm: the serial sum, or over a partition the
+    // exact sum of this range's products across the ranks.
+    double gdot(const std::vector<double> &a, const std::vector<double> &b)
+    {
+        if (!part_) return dotv(a, b);
+        ExactSum s;
+        for (size_t i = 6 * nlo(); i < 6 * nhi(); ++i) s.add(a[i] * b[i]);
+        return all_sum(s);
+    }
+    double gnorm(const std::vector<double> &a) { return std::sqrt(gdot(a, a)); }
 
     // cuda_backend.cu:815-841
     void build_preconditioner(double dt)
     {
         const KhsHairMaterial &m = material_;
         const double inv = 1.0 / dt, inv2 = inv * inv;
-        for (size_t n = 0; n < N(); ++n) {
+        for (size_t n = nlo(); n < nhi(); ++n) {
             const double p = nodes_[n].mass * (inv2 + m.mass_damping * inv);
             const double r = nodes_[n].rmass * (inv2 + m.mass_damping * inv);
             for (int d = 0; d < 3; ++d) { precond_[6 * n + d] = p; precond_[6 * n + 3 + d] = r; }
@@ -1540,7 +1711,8 @@ private:
         const double area = kPi * m.radius * m.radius;
         const double inertia = kPi * m.radius * m.radius * m.radius * m.radius / 4.0;
         const double G = m.young_modulus / (2.0 * (1.0 + m.poisson_ratio));
-        for (const Element &e : elements_) {
+        for (size_t ei = elo(); ei < ehi(); ++ei) {
+            const Element &e = elements_[ei];
             const double tr = std::fmax(m.young_modulus * area, m.shear_correction * G * area) / e.L0;
             const double rot = m.shear_correction * G * area * e.L0 + std::fmax(m.young_modulus * inertia, 2.0 * G * inertia) / e.L0;
             for (int d = 0; d < 3; ++d) {
@@ -1548,7 +1720,7 @@ private:
                 precond_[6 * e.i + 3 + d] += rot; precond_[6 * e.j + 3 + d] += rot;
             }
         }
-        for (size_t n = 0; n < N(); ++n)
+        for (size_t n = nlo(); n < nhi(); ++n)
             for (int d = 0; d < 6; ++d) precond_[6 * n + d] = nodes_[n].fixed ? 0.0 : 1.0 / std::fmax(precond_[6 * n + d], 1.0e-30);
     }
 
@@ -1556,13 +1728,14 @@ private:
     void limit_direction()
     {
         double mx = 0.0;
-        for (size_t n = 0; n < N(); ++n) {
+        for (size_t n = nlo(); n < nhi(); ++n) {
             if (nodes_[n].fixed) continue;
             mx = std::fmax(mx, norm(v3(dir_[6 * n], dir_[6 * n + 1], dir_[6 * n + 2])));
         }
+        mx = all_max(mx);
         if (mx > trust_radius_) {
             const double scale = trust_radius_ / mx;
-            for (double &x : dir_) x *= scale;
+            for (size_t i = 6 * nlo(); i < 6 * nhi(); ++i) dir_[i] *= scale;
             ++trust_;
         }
     }
@@ -1570,8 +1743,8 @@ private:
     // cuda_backend.cu:632-638
     void make_steepest()
     {
-        for (size_t i = 0; i < dof(); ++i) dir_[i] = -grad_[i] * precond_[i];
-        for (size_t n = 0; n < N(); ++n) if (nodes_[n].fixed) for (int d = 0; d < 6; ++d) dir_[6 * n + d] = 0.0;
+        for (size_t i = 6 * nlo(); i < 6 * nhi(); ++i) dir_[i] = -grad_[i] * precond_[i];
+        for (size_t n = nlo(); n < nhi(); ++n) if (nodes_[n].fixed) for (int d = 0; d < 6; ++d) dir_[6 * n + d] = 0.0;
         limit_direction();
     }
 
@@ -1580,7 +1753,7 @@ private:
     {
         const bool ok = block_solve();
         bool used = false;
-        if (ok) { const double slope = dotv(grad_, dir_); used = slope < 0 && std::isfinite(slope); }
+        if (ok) { const double slope = gdot(grad_, dir_); used = slope < 0 && std::isfinite(slope); }
         if (!used) { ++steepest_; make_steepest(); return false; }
         limit_direction();
         return true;
@@ -1593,7 +1766,7 @@ private:
         const double target = m.radius + m.collider_offset + desc_.minimum_gap;
         std::vector<double> lim(E(), 1.0);
 #pragma omp parallel for schedule(dynamic, 64)
-        for (long long ei = 0; ei < (long long)E(); ++ei) {
+        for (long long ei = (long long)elo(); ei < (long long)ehi(); ++ei) {
             const Element &e = elements_[size_t(ei)];
             if (nodes_[e.i].fixed || !e.contact) continue;
             const V3 p0 = pos(e.i), p1 = pos(e.j);
@@ -1621,7 +1794,38 @@ private:
         }
         double alpha = 1.0;
         for (double l : lim) alpha = std::fmin(alpha, l);
-        return alpha;
+        return all_min(alpha);
+    }
+
+    // Partitioned sweep result: the failure with the lowest element index
+    // over all ranks, its record sent by the rank that owns the element
+    // (every other rank adds zeros to the integer sum of the record's bits).
+    bool sweep_result(const std::vector<SweepFailure> &per, SweepFailure &fail_out)
+    {
+        int64_t first = std::numeric_limits<int64_t>::max();
+        for (size_t ei = elo(); ei < ehi(); ++ei)
+            if (per[ei].claimed) { first = int64_t(ei); break; }
+        first = all_int(first, 1);
+        if (first == std::numeric_limits<int64_t>::max()) return true;
+        const bool mine = size_t(first) >= elo() && size_t(first) < ehi();
+        const SweepFailure &f = per[mine ? size_t(first) : 0];
+        const double d[13] = {f.distance, f.required, f.clearance, f.displacement, f.hair_start.x, f.hair_start.y,
+                              f.hair_start.z, f.hair_end.x, f.hair_end.y, f.hair_end.z, f.collider_point.x,
+                              f.collider_point.y, f.collider_point.z};
+        int64_t rec[16] = {};
+        if (mine) {
+            rec[0] = f.strand; rec[1] = f.element; rec[2] = f.triangle;
+            std::memcpy(rec + 3, d, sizeof(d));
+        }
+        reduce_(reduce_ctx_, rec, 16, 0);
+        double o[13];
+        std::memcpy(o, rec + 3, sizeof(o));
+        fail_out.claimed = true;
+        fail_out.strand = uint32_t(rec[0]); fail_out.element = uint32_t(rec[1]); fail_out.triangle = uint32_t(rec[2]);
+        fail_out.distance = o[0]; fail_out.required = o[1]; fail_out.clearance = o[2]; fail_out.displacement = o[3];
+        fail_out.hair_start = v3(o[4], o[5], o[6]); fail_out.hair_end = v3(o[7], o[8], o[9]);
+        fail_out.collider_point = v3(o[10], o[11], o[12]);
+        return false;
     }
 
     // Moving-collider conservative advancement (cuda_backend.cu:966-987).
@@ -1631,7 +1835,7 @@ private:
         const double target = m.radius + m.collider_offset + desc_.minimum_gap;
         std::vector<SweepFailure> per(E());
 #pragma omp parallel for schedule(dynamic, 64)
-        for (long long ei = 0; ei < (long long)E(); ++ei) {
+        for (long long ei = (long long)elo(); ei < (long long)ehi(); ++ei) {
             const Element &e = elements_[size_t(ei)];
             if (nodes_[e.i].fixed || !e.contact) continue;
             const V3 p0 = pos(e.i), p1 = pos(e.j);
@@ -1667,6 +1871,7 @@ private:
                 if (!end) record();
             });
         }
+        if (part_) return sweep_result(per, fail_out);
         for (size_t ei = 0; ei < E(); ++ei)
             if (per[ei].claimed) { fail_out = per[ei]; return false; }
         return true;
@@ -1680,7 +1885,7 @@ private:
         struct Imp { bool any = false; double di[3] = {0, 0, 0}, dj[3] = {0, 0, 0}; };
         std::vector<Imp> imp(E());
 #pragma omp parallel for schedule(dynamic, 64)
-        for (long long ei = 0; ei < (long long)E(); ++ei) {
+        for (long long ei = (long long)elo(); ei < (long long)ehi(); ++ei) {
             const Element &e = elements_[size_t(ei)];
             if (!e.contact) continue;
             if (nodes_[e.i].fixed && nodes_[e.j].fixed) continue;
@@ -1721,19 +1926,19 @@ private:
             if (!nodes_[e.j].fixed) { const double s = w1 / std::fmax(nodes_[e.j].mass, 1.0e-30); o.dj[0] = impulse.x * s; o.dj[1] = impulse.y * s; o.dj[2] = impulse.z * s; }
         }
         std::vector<double> dv(dof(), 0.0);
-        for (size_t ei = 0; ei < E(); ++ei) {
+        for (size_t ei = elo(); ei < ehi(); ++ei) {
             const Imp &o = imp[ei];
             if (!o.any) continue;
             const Element &e = elements_[ei];
             for (int d = 0; d < 3; ++d) { dv[6 * e.i + d] += o.di[d]; dv[6 * e.j + d] += o.dj[d]; }
         }
-        for (size_t i = 0; i < dof(); ++i) v_[i] += dv[i];
+        for (size_t i = 6 * nlo(); i < 6 * nhi(); ++i) v_[i] += dv[i];
     }
 
     void update_velocity(double dt)
     {
         const double inv_dt = 1.0 / dt;
-        for (size_t n = 0; n < N(); ++n) {
+        for (size_t n = nlo(); n < nhi(); ++n) {
             if (nodes_[n].fixed) continue;
             for (int d = 0; d < 6; ++d) v_[6 * n + d] = (q_[6 * n + d] - old_q_[6 * n + d]) * inv_dt;
         }
@@ -1745,12 +1950,12 @@ private:
         build_preconditioner(dt);
         Stats current = evaluate(true, dt);
         if (!current.feasible) return fail(KHS_ERROR_NOT_CONVERGED, "state is outside the barrier feasible region");
-        const double initial = nrm2(grad_);
+        const double initial = gnorm(grad_);
         step_stats_.initial_residual_norm = std::fmax(step_stats_.initial_residual_norm, initial);
         for (uint32_t it = 0; it <= desc_.newton_iterations; ++it) {
             progress_iteration_.store(it);
-            if (cancel_.load()) return fail(KHS_ERROR_INVALID_STATE, "solve cancelled");
-            const double residual = nrm2(grad_);
+            if (all_int(cancel_.load() ? 1 : 0, 2)) return fail(KHS_ERROR_INVALID_STATE, "solve cancelled");
+            const double residual = gnorm(grad_);
             const double relative = residual / std::fmax(initial, 1e-30);
             step_stats_.final_residual_norm = residual;
             step_stats_.relative_residual_norm = relative;
@@ -1778,7 +1983,7 @@ private:
             bool accepted = false;
             double alpha = 1.0;
             for (int attempt = 0; attempt < 2; ++attempt) {
-                const double slope = dotv(grad_, dir_);
+                const double slope = gdot(grad_, dir_);
                 alpha = 1.0;
                 if (has_collider()) {
                     progress_phase_.store(KHS_PHASE_CCD);
@@ -1790,7 +1995,7 @@ private:
                 progress_phase_.store(KHS_PHASE_LINE_SEARCH);
                 if (alpha >= desc_.minimum_line_search_step)
                     for (uint32_t s = 0; s < desc_.line_search_iterations; ++s) {
-                        for (size_t i = 0; i < dof(); ++i) q_[i] = base_q_[i] + alpha * dir_[i];
+                        for (size_t i = 6 * nlo(); i < 6 * nhi(); ++i) q_[i] = base_q_[i] + alpha * dir_[i];
                         const Stats trial = evaluate(false, dt);
                         ++step_stats_.line_search_evaluations;
                         ++rec.line_search_evaluations;
@@ -1810,7 +2015,7 @@ private:
             }
             if (!accepted) { q_ = base_q_; return fail(KHS_ERROR_NOT_CONVERGED, "Gauss-Newton line search failed"); }
             current = evaluate(true, dt);
-            const double dnorm = nrm2(dir_);
+            const double dnorm = gnorm(dir_);
             step_stats_.increment_norm = alpha * dnorm;
             step_stats_.accepted_step_length = alpha;
             ++step_stats_.newton_iterations;
@@ -1879,7 +2084,7 @@ private:
                 trust_ = 0;
                 old_q_ = q_;
                 const double f = double(sub) / substeps;
-                for (size_t n = 0; n < N(); ++n) {
+                for (size_t n = nlo(); n < nhi(); ++n) {
                     if (!nodes_[n].fixed) continue;
                     const V3 p = root_a[n] * (1.0 - f) + root_b[n] * f, r = rot_a[n] * (1.0 - f) + rot_b[n] * f;
                     const double vals[6] = {p.x, p.y, p.z, r.x, r.y, r.z};
@@ -1973,6 +2178,42 @@ private:
     std::vector<KhsxContactRecord> contact_records_;
     std::vector<KhsxSubstepRecord> records_;
     uint32_t substep_limit_ = 0;  // khsxSetSubstepLimit (0: whole frames)
+    // Strand partition (set_partition): the node, element and strand ranges
+    // stepped here, and the all-reduce that combines the global scalars.
+    bool part_ = false;
+    size_t n_lo_ = 0, n_hi_ = 0, e_lo_ = 0, e_hi_ = 0, s_lo_ = 0, s_hi_ = 0;
+    ReduceFn reduce_ = nullptr;
+    void *reduce_ctx_ = nullptr;
+    size_t nlo() const { return part_ ? n_lo_ : 0; }
+    size_t nhi() const { return part_ ? n_hi_ : N(); }
+    size_t elo() const { return part_ ? e_lo_ : 0; }
+    size_t ehi() const { return part_ ? e_hi_ : E(); }
+    size_t slo() const { return part_ ? s_lo_ : 0; }
+    size_t shi() const { return part_ ? s_hi_ : strands_.size(); }
+    int64_t all_int(int64_t x, int op)
+    {
+        if (part_) reduce_(reduce_ctx_, &x, 1, op);
+        return x;
+    }
+    double all_min(double x)
+    {
+        if (!part_) return x;
+        int64_t k = order_key(x);
+        reduce_(reduce_ctx_, &k, 1, 1);
+        return from_order_key(k);
+    }
+    double all_max(double x)
+    {
+        if (!part_) return x;
+        int64_t k = order_key(x);
+        reduce_(reduce_ctx_, &k, 1, 2);
+        return from_order_key(k);
+    }
+    double all_sum(ExactSum &s)
+    {
+        reduce_(reduce_ctx_, s.v, ExactSum::kSize, 0);
+        return s.value();
+    }
     uint32_t steepest_ = 0, trust_ = 0;  // per substep: steepest fallbacks, trust-radius scalings
     double max_rest_length_ = 0.0, trust_radius_ = 0.0, last_frame_ms_ = 0.0;
     bool animation_ready_ = false;
@@ -2143,6 +2384,13 @@ KHS_API void khsOracleExportModel(const KhsSolver *s, double *node_f, uint32_t *
                                   uint32_t *strand_u, uint32_t *mapping, double *collider, uint32_t *tris)
 {
     if (s) s->impl.export_model(node_f, node_u, elem_f, elem_u, strand_u, mapping, collider, tris);
+}
+
+// Oracle-only test hook (see Solver::set_partition): step only strands
+// [s0, s1) and combine the global scalars through `reduce`.
+KHS_API KhsResult khsOracleSetPartition(KhsSolver *s, uint32_t s0, uint32_t s1, khs_oracle::ReduceFn reduce, void *ctx)
+{
+    return s ? s->impl.set_partition(s0, s1, reduce, ctx) : KHS_ERROR_INVALID_ARGUMENT;
 }
 
 // Oracle-only: stop every frame after n substeps (0 = whole frames).

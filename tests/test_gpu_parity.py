@@ -183,12 +183,12 @@ def test_mixed_ff_sphere_moving(gpu_lib, oracle_lib):
 
 def test_block_solve_layouts_bit_identical(gpu_lib):
     """Every block-solve launch shape (5 strands of 6 lanes, 2 of 12 or 1 of
-    18 lanes per warp, the longest strands on 18 lanes and the rest five per
-    warp, any number of blocks per SM) gives bit-identical
+    18 lanes per warp, the longest strands on 18 lanes or on a pair of warps
+    and the rest five per warp, any number of blocks per SM) gives bit-identical
     trajectories, so the one-time launch tuning cannot change a result."""
     sc = scenes.ellipsoid_scene(strands=200, frames=2)
     finals = []
-    for spw, bps, nlong in ((5, 1, 0), (2, 1, 0), (2, 3, 0), (5, 4, 0), (1, 1, 0), (5, 2, 17)):
+    for spw, bps, nlong in ((5, 1, 0), (2, 1, 0), (2, 3, 0), (5, 4, 0), (1, 1, 0), (5, 2, 17), (1, 1, 17), (1, 2, 40)):
         s = kn.HairSolver(gpu_lib)
         scenes.load_into(s, sc)
         s.set_block_solve_schedule(spw, bps, nlong)
