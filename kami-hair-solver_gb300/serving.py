@@ -7,7 +7,12 @@ one process on one GPU:
   free and its device bytes fit the remaining HBM budget (first fit in
   arrival order); finished requests return their slot and bytes at once, so
   requests that arrive while others run join the mix without waiting for a
-  batch boundary.
+  batch boundary.  A request reserves a conservative upper bound of its
+  bytes (``estimate_bytes``) while it builds; once its solver is resident
+  (model, animation frames and rollback ring on the device) the reservation
+  is replaced by the bytes the solver itself reports
+  (``KhsGpuStats.resident_bytes``, plus its peak temporary bytes), and the
+  difference goes back to the budget at once.
 * Residency: each admitted request builds its own solver, which keeps the
   rod state, the Gauss-Newton blocks, the BVH and every animation frame in
   one device arena on its own CUDA stream, plus a device-resident rollback
@@ -42,8 +47,9 @@ import numpy as np
 import khs_native as kn
 import scenes
 
-# Conservative device bytes of a solver: the arena (state, blocks, factors,
-# contact and BVH arrays), every animation frame, and the rollback ring.
+# Conservative device bytes of a solver before it is built: the arena (state,
+# blocks, factors, contact and BVH arrays), every animation frame, and the
+# rollback ring.  Used only until the built solver reports its own bytes.
 BYTES_PER_NODE = 4096
 BYTES_PER_TRIANGLE = 1024
 RING_BYTES_PER_NODE = 96
@@ -74,14 +80,25 @@ class Result:
     frame_ms: list = dataclasses.field(default_factory=list)
     substeps: list = dataclasses.field(default_factory=list)
     nodes: int = 0
-    bytes: int = 0
+    bytes: int = 0          # bytes reserved at admission (the estimate)
+    resident: int = 0       # bytes the built solver reported
     arrival: float = 0.0
     admitted: float = 0.0
     finished: float = 0.0
 
 
-def run_request(lib, req: Request, mode: int, ring_slots: int) -> Result:
-    """Builds and steps one request on the calling thread."""
+def resident_bytes(solver: kn.HairSolver) -> int:
+    """Device bytes a built solver holds: its resident arrays (model, state,
+    animation frames, rollback ring) and its peak temporary allocation."""
+    g = solver.gpu_stats()
+    return int(g.resident_bytes) + int(g.peak_temporary_bytes)
+
+
+def run_request(lib, req: Request, mode: int, ring_slots: int, on_resident=None) -> Result:
+    """Builds and steps one request on the calling thread.  ``on_resident``
+    (if given) is called with the solver's own device bytes once it is
+    built, its frames uploaded and its ring allocated, before the first
+    frame is stepped."""
     res = Result(rid=req.rid, arrival=req.arrival)
     s = kn.HairSolver(lib)
     try:
@@ -90,6 +107,9 @@ def run_request(lib, req: Request, mode: int, ring_slots: int) -> Result:
         if ring_slots and hasattr(s._library, "khsxSetRollbackRing"):
             s.set_rollback_ring(ring_slots)
         res.nodes = int(s.build_stats().internal_node_count)
+        res.resident = resident_bytes(s)
+        if on_resident is not None:
+            on_resident(res.resident)
         for f in range(1, req.frames + 1):
             t0 = time.perf_counter()
             r = s._library.khsStepAnimationFrame(s.handle, f, req.scene.frame_dt)
@@ -110,8 +130,9 @@ class Server:
     """Admits requests by slot and HBM budget and runs them concurrently."""
 
     def __init__(self, lib, budget_bytes: int, max_slots: int = 8, mode: int = kn.MODE_MIXED, ring_slots: int = 10,
-                 estimate=estimate_bytes):
+                 estimate=estimate_bytes, runner=run_request):
         self.lib = lib
+        self.runner = runner
         self.budget = int(budget_bytes)
         self.max_slots = int(max_slots)
         self.mode = mode
@@ -129,12 +150,22 @@ class Server:
         threads = []
 
         def worker(req: Request, nbytes: int, admitted: float):
-            res = run_request(self.lib, req, self.mode, self.ring_slots)
+            held = {"bytes": nbytes}
+
+            def on_resident(actual: int):
+                # Replace the reservation by the solver's own bytes.
+                with lock:
+                    used["bytes"] += actual - held["bytes"]
+                    held["bytes"] = actual
+                    self.peak_bytes = max(self.peak_bytes, used["bytes"])
+                    lock.notify_all()
+
+            res = self.runner(self.lib, req, self.mode, self.ring_slots, on_resident)
             res.bytes, res.admitted = nbytes, admitted
             res.finished = time.perf_counter() - start
             with lock:
                 results[req.rid] = res
-                used["bytes"] -= nbytes
+                used["bytes"] -= held["bytes"]
                 used["slots"] -= 1
                 lock.notify_all()
 
@@ -163,8 +194,9 @@ class Server:
                         admitted_any = True
                 if admitted_any:
                     continue
-                # Sleep until the next arrival or until a running request
-                # finishes (its worker notifies), whichever comes first.
+                # Sleep until the next arrival, until a running request
+                # finishes or reports its resident bytes (its worker
+                # notifies), whichever comes first.
                 now = time.perf_counter() - start
                 future = [r.arrival for r in waiting if r.arrival > now]
                 lock.wait(timeout=(min(future) - now) if future else None)
@@ -202,6 +234,8 @@ def summary(results: list[Result], makespan: float) -> dict:
         "node_substeps_per_s": node_substeps / makespan if makespan > 0 else None,
         "makespan_s": makespan,
         "mean_queue_s": statistics.fmean(r.admitted - r.arrival for r in results) if results else None,
+        "reserved_bytes_total": sum(r.bytes for r in results),
+        "resident_bytes_total": sum(r.resident for r in results),
     }
 
 

@@ -40,3 +40,42 @@ def test_request_over_budget_is_rejected(oracle_lib):
     res = server.run(reqs)
     assert res[0].status == kn.OK
     assert res[1].status == kn.ERROR_INVALID_ARGUMENT and "budget" in res[1].error
+
+
+def _fake_runner(actual, hold_s):
+    """A request runner that reports ``actual`` resident bytes once built
+    and then occupies its slot for ``hold_s`` seconds."""
+    import time
+
+    def run(lib, req, mode, ring_slots, on_resident=None):
+        if on_resident is not None:
+            on_resident(actual)
+        time.sleep(hold_s)
+        return serving.Result(rid=req.rid, frame_ms=[1.0], substeps=[8], nodes=10, resident=actual)
+    return run
+
+
+def test_admission_uses_the_solvers_reported_bytes():
+    """A request reserves its estimate while it builds and then holds only
+    the bytes its solver reports, so a second request that did not fit next
+    to the first one's estimate is admitted while the first still runs."""
+    reqs = [serving.Request(rid=i, scene=None, arrival=0.0, frames=1) for i in range(2)]
+    estimate = lambda scene, ring: 6  # noqa: E731
+    server = serving.Server(None, budget_bytes=10, max_slots=4, estimate=estimate, runner=_fake_runner(3, 0.3))
+    res = server.run(reqs)
+    assert all(r.status == kn.OK for r in res)
+    assert server.peak_slots == 2  # 3 reported + 6 reserved fit in 10
+    assert server.peak_bytes <= 10
+    # With the estimate held for the whole run the two never overlap.
+    server = serving.Server(None, budget_bytes=10, max_slots=4, estimate=estimate, runner=_fake_runner(6, 0.1))
+    server.run(reqs)
+    assert server.peak_slots == 1
+
+
+def test_reported_bytes_above_the_estimate_hold_back_admission():
+    reqs = [serving.Request(rid=i, scene=None, arrival=0.0, frames=1) for i in range(3)]
+    server = serving.Server(None, budget_bytes=10, max_slots=4, estimate=lambda scene, ring: 4,
+                            runner=_fake_runner(7, 0.2))
+    res = server.run(reqs)
+    assert all(r.status == kn.OK for r in res)
+    assert len(res) == 3 and server.peak_slots <= 2
