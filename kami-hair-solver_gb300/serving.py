@@ -39,6 +39,7 @@ import argparse
 import dataclasses
 import json
 import statistics
+import sys
 import threading
 import time
 
@@ -130,9 +131,10 @@ class Server:
     """Admits requests by slot and HBM budget and runs them concurrently."""
 
     def __init__(self, lib, budget_bytes: int, max_slots: int = 8, mode: int = kn.MODE_MIXED, ring_slots: int = 10,
-                 estimate=estimate_bytes, runner=run_request):
+                 estimate=estimate_bytes, runner=run_request, on_result=None):
         self.lib = lib
         self.runner = runner
+        self.on_result = on_result  # called with each finished Result (from its worker thread)
         self.budget = int(budget_bytes)
         self.max_slots = int(max_slots)
         self.mode = mode
@@ -163,6 +165,8 @@ class Server:
             res = self.runner(self.lib, req, self.mode, self.ring_slots, on_resident)
             res.bytes, res.admitted = nbytes, admitted
             res.finished = time.perf_counter() - start
+            if self.on_result is not None:
+                self.on_result(res)
             with lock:
                 results[req.rid] = res
                 used["bytes"] -= held["bytes"]
@@ -267,19 +271,40 @@ def main() -> None:
     ap.add_argument("--ring", type=int, default=10)
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--serial-plain", action="store_true", help="also run the stream one at a time in plain FP64")
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="also run the first N requests of the stream (same seeds, same arrivals) batched in the "
+                         "mixed form and one at a time in plain FP64, for a like-for-like comparison")
     args = ap.parse_args()
     lib = kn.Library(khs_build.build())
     reqs = make_stream(args.requests, args.rate, args.seed, strand_range=(args.min_strands, args.max_strands),
                        frames=args.frames)
-    server = Server(lib, int(args.budget_gb * 1e9), args.slots, kn.MODE_MIXED, args.ring)
+    def progress(r: Result) -> None:
+        # One write per line: workers finish concurrently.
+        sys.stderr.write(json.dumps({"rid": r.rid, "status": r.status, "nodes": r.nodes, "substeps": sum(r.substeps),
+                                     "frame_ms": [round(x, 1) for x in r.frame_ms], "arrival": round(r.arrival, 3),
+                                     "admitted": round(r.admitted, 3), "finished": round(r.finished, 3),
+                                     "resident_bytes": r.resident}) + "\n")
+        sys.stderr.flush()
+
+    server = Server(lib, int(args.budget_gb * 1e9), args.slots, kn.MODE_MIXED, args.ring, on_result=progress)
     res = server.run(reqs)
     line = {"workload": f"{args.requests} requests, Poisson {args.rate}/s, strands log-U[{args.min_strands}, "
                         f"{args.max_strands}], {args.frames} frames x 8 substeps",
             "mixed_batched": summary(res, server.makespan), "peak_budget_bytes": server.peak_bytes,
             "peak_slots": server.peak_slots}
+    print(json.dumps(line), flush=True)
     if args.serial_plain:
         sres, span = run_serial(lib, reqs, kn.MODE_PLAIN_FP64)
         line["plain_serial"] = summary(sres, span)
+    if args.plain_sample:
+        sample = reqs[:args.plain_sample]
+        sserver = Server(lib, int(args.budget_gb * 1e9), args.slots, kn.MODE_MIXED, args.ring)
+        sres = sserver.run(sample)
+        pres, span = run_serial(lib, sample, kn.MODE_PLAIN_FP64, args.ring)
+        line["sample"] = {"requests": len(sample), "mixed_batched": summary(sres, sserver.makespan),
+                          "plain_serial": summary(pres, span),
+                          "same_final_state": all(a.q is not None and b.q is not None and (a.q == b.q).all()
+                                                  for a, b in zip(sres, pres))}
     print(json.dumps(line), flush=True)
 
 
