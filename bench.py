@@ -83,8 +83,16 @@ MEASURED_PEAKS = REPO / "MEASURED_PEAKS.json"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # dominant kernels from one ncu capture of this workload; see profiles/.
 # (k_block_solve's traffic does not depend on the contact state.)
-NCU_TRAFFIC_BYTES: dict[str, float] = {"k_block_solve": 181.063424e6 + 64.278016e6,
+NCU_TRAFFIC_BYTES: dict[str, float] = {"k_block_solve": 195.529728e6 + 69.514496e6,
                                       "k_elem_eval_grad": 89.102592e6 + 211.5456e6}
+
+# FP64 operations per unit that the element and node kernels execute (dadd +
+# dmul + 2 dfma, thread level, predicated-on), counted by ncu on the body
+# scene (profiles/fp64_op_counts_body_scene.md).  The reference method
+# differentiates with Dual<12>; these count this implementation's
+# closed-form arithmetic, which is the work the FP64 pipe has to do.
+COUNTED_FLOPS = {"k_elem_eval_grad": 1089.0, "k_elem_eval_energy": 152.0,
+                 "k_node_eval_grad": 365.0, "k_node_eval_energy": 256.0}
 
 
 def algorithmic(name: str, nodes: int, free_nodes: int, elements: int, candidates: float):
@@ -108,15 +116,21 @@ def algorithmic(name: str, nodes: int, free_nodes: int, elements: int, candidate
       the upper block (288 B).
     * k_node_eval_*, per node: q, q_old, v (144 B), constants (88 B),
       gradient and diagonal written (48 + 48 B).
+    * k_elem_eval_energy, per element: q and R of both nodes (96 + 144 B),
+      constants (56 B), the two energies written (16 B).
+    FP64 flops of k_elem_eval_* and k_node_eval_* are the counted ones
+    (COUNTED_FLOPS).
     """
     if name == "k_block_solve":
         return 672.0 * free_nodes, 1872.0 * free_nodes
     if name in ("k_contact", "k_contact_query"):
         return 115.0 * elements + 84.0 * candidates, None
     if name == "k_elem_eval_grad":
-        return 1400.0 * elements, None
+        return 1400.0 * elements, COUNTED_FLOPS[name] * elements
+    if name == "k_elem_eval_energy":
+        return 312.0 * elements, COUNTED_FLOPS[name] * elements
     if name.startswith("k_node_eval"):
-        return 328.0 * nodes, None
+        return 328.0 * nodes, COUNTED_FLOPS.get(name, 0.0) * nodes or None
     return None, None
 
 
@@ -480,6 +494,18 @@ def _roofline(run: dict, fp64_peak: float) -> dict:
         roof["hbm"] = hbm
     elif fp64:
         roof["fp64"] = fp64
+    # The next kernels by share, against the same FP64 roof.
+    others = {}
+    for other, (n_other, ms_other) in sorted(timings.items(), key=lambda kv: -kv[1][1])[1:4]:
+        b_other, f_other = algorithmic(other, nodes, free_nodes, elements, cand_per_eval)
+        t_other = (ms_other / max(n_other, 1)) / 1e3
+        if f_other and t_other > 0:
+            tf = f_other / t_other / 1e12
+            others[other] = {"avg_launch_ms": round(ms_other / max(n_other, 1), 4), "share": round(ms_other / total, 4),
+                             "fp64_tflops": round(tf, 4), "fp64_frac": round(tf / fp64_peak, 4),
+                             "hbm_gbs": round(b_other / t_other / 1e9, 1) if b_other else None}
+    if others:
+        roof["next_kernels"] = others
     return roof
 
 

@@ -420,6 +420,19 @@ KHS_API uint32_t khsxGetSolveMode(const KhsSolver *solver);
 KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *solver, uint32_t strands_per_warp, uint32_t blocks_per_sm,
                                             uint32_t long_strands);
 
+/* Tiered launch shape of the FP64 block-tridiagonal solve (the tuner also
+   considers it): the `quads` longest strands each on four warps of one
+   block (one warp runs the pivot steps on the diagonal blocks, three apply
+   them to two columns each of the coupling blocks and the right-hand side
+   and form the next Schur complement), the next `singles` strands one per
+   warp (18 lanes), the next `doubles` two per warp (12 lanes each), the rest
+   five per warp; blocks_per_sm 1-8; quads + singles + doubles must not
+   exceed the strand count.  Every shape gives bit-identical directions.
+   No counterpart in the reference (its solve is one thread per strand,
+   src/cuda_backend.cu:866-881).  Requires a built solver. */
+KHS_API KhsResult khsxSetBlockSolveTiers(KhsSolver *solver, uint32_t quads, uint32_t singles, uint32_t doubles,
+                                         uint32_t blocks_per_sm);
+
 /* Device-resident rollback ring: the rod state (q and v) after each of the
    last `slots` successful animation frames stays in device memory (2 x 48
    bytes per internal node per slot), so a serving loop can rewind a bake

@@ -676,6 +676,15 @@ KHS_API KhsResult khsxSetBlockSolveSchedule(KhsSolver *s, uint32_t strands_per_w
     });
 }
 
+KHS_API KhsResult khsxSetBlockSolveTiers(KhsSolver *s, uint32_t quads, uint32_t singles, uint32_t doubles,
+                                         uint32_t blocks_per_sm)
+{
+    return guarded(s, [&] {
+        if (!s->built || !s->engine) return KHS_ERROR_INVALID_STATE;
+        return s->engine->set_block_solve_tiers(quads, singles, doubles, blocks_per_sm);
+    });
+}
+
 KHS_API KhsResult khsxCopyState(const KhsSolver *s, double *q, double *v, uint64_t dof_capacity)
 {
     if (!s || !s->built || !s->engine) return KHS_ERROR_INVALID_ARGUMENT;

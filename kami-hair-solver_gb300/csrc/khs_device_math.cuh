@@ -13,6 +13,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 #if defined(__CUDACC__)
 #define KHS_HD __host__ __device__ __forceinline__
@@ -696,6 +697,102 @@ KHS_HD V rotation_vector(const M &r)
     if (!gfinite(angle) || !gfinite(axis.x) || !gfinite(axis.y) || !gfinite(axis.z)) return v(0.0, 0.0, 0.0);
     if (angle > kPi) angle = xs(angle, xm(2.0, kPi));
     return gmul(axis, angle);
+}
+
+// ---- correctly rounded reciprocal on the integer pipes -----------------
+//
+// 1/x rounded to nearest, computed without FP64 instructions: on GB300 one
+// FP64 warp instruction occupies a sub-partition's pipe for ~64 cycles, and
+// the block solve's pivot warp is bound by its FP64 instruction count.
+// For x = (-1)^s * M * 2^(E-1075) with M the 53-bit significand,
+// 1/x = (-1)^s * (2^105 / M) * 2^(970-E).  T = 2^105 / M lies in
+// (2^52, 2^53]:
+// * seed: an FP32 reciprocal of the top 24 bits of M, scaled to T0 ~ T
+//   (relative error below 2^-21);
+// * one residual step of order three: e = (2^105 - T0 M) / 2^105 in 64-bit
+//   fixed point, T1 = T0 (1 + e + e^2), error of order e^3 plus truncation
+//   (a few units);
+// * exact remainder R = 2^105 - T1 M (the low 64 bits suffice: |R| < 2^63)
+//   brings T1 to floor(T) with 0 <= R < M; the nearest integer is floor(T)
+//   + (2R > M) (no ties: M > 1 is odd or a power of two);
+// * reciprocals below the normal range (|x| >= 2^1022) are rounded from
+//   floor(T) and R to nearest-even.
+// The result equals the IEEE division 1.0 / x for every finite nonzero x
+// (checked bit for bit against __drcp_rn on 2^31 values on GB300 and
+// against 1.0 / x on the host, tests/native/test_recip.cpp); zero,
+// subnormal and non-finite inputs give an unspecified finite bit pattern
+// (the block solve fails such pivots before using the result).
+#if defined(__CUDA_ARCH__)
+KHS_HD uint64_t umulhi64(uint64_t a, uint64_t b) { return __umul64hi(a, b); }
+KHS_HD int64_t smulhi64(int64_t a, int64_t b) { return __mul64hi(a, b); }
+KHS_HD float recip_seed(float m)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(m));
+    return r;
+}
+KHS_HD uint64_t bits_of(double x) { return uint64_t(__double_as_longlong(x)); }
+KHS_HD double double_of(uint64_t b) { return __longlong_as_double((long long)b); }
+KHS_HD uint32_t bits_of(float x) { return __float_as_uint(x); }
+KHS_HD float float_of(uint32_t b) { return __uint_as_float(b); }
+#else
+KHS_HD uint64_t umulhi64(uint64_t a, uint64_t b) { return uint64_t((unsigned __int128)a * b >> 64); }
+KHS_HD int64_t smulhi64(int64_t a, int64_t b) { return int64_t((__int128)a * b >> 64); }
+// Host seed: the correctly rounded float reciprocal (tests may substitute a
+// perturbed one through KHS_RECIP_SEED_HOST).
+#ifndef KHS_RECIP_SEED_HOST
+#define KHS_RECIP_SEED_HOST(m) (1.0f / (m))
+#endif
+KHS_HD float recip_seed(float m) { return KHS_RECIP_SEED_HOST(m); }
+KHS_HD uint64_t bits_of(double x) { uint64_t b; std::memcpy(&b, &x, 8); return b; }
+KHS_HD double double_of(uint64_t b) { double x; std::memcpy(&x, &b, 8); return x; }
+KHS_HD uint32_t bits_of(float x) { uint32_t b; std::memcpy(&b, &x, 4); return b; }
+KHS_HD float float_of(uint32_t b) { float x; std::memcpy(&x, &b, 4); return x; }
+#endif
+
+KHS_HD double recip_rn(double x)
+{
+    const uint64_t b = bits_of(x);
+    const uint64_t sign = b & 0x8000000000000000ull;
+    const int E = int((b >> 52) & 0x7ff);
+    const uint64_t M = (b & 0xfffffffffffffull) | (1ull << 52);
+    const uint32_t rb = bits_of(recip_seed(float_of((127u << 23) | uint32_t((M >> 29) & 0x7fffff))));
+    const int er = int((rb >> 23) & 0xff) - 127;  // the seed lies in (0.5, 1]: -1 or 0
+    const uint64_t T0 = uint64_t((rb & 0x7fffff) | 0x800000) << (30 + er);
+    const uint64_t Plo = T0 * M, Phi = umulhi64(T0, M);
+    const uint64_t Rlo = 0 - Plo;
+    const uint64_t Rhi = (1ull << 41) - Phi - uint64_t(Plo != 0);
+    const int64_t e = int64_t((Rhi << 23) | (Rlo >> 41));  // (2^105 - T0 M) / 2^41
+    const uint64_t ae = e < 0 ? uint64_t(-e) : uint64_t(e);
+    const int64_t s = e + int64_t(umulhi64(ae, ae));
+    uint64_t T1 = T0 + uint64_t(smulhi64(int64_t(T0), s));
+    int64_t R = int64_t(0 - T1 * M);
+    for (int k = 0; k < 2; ++k) {
+        const bool low = R < 0;
+        T1 -= uint64_t(low);
+        R += low ? int64_t(M) : 0;
+    }
+    for (int k = 0; k < 2; ++k) {
+        const bool high = R >= int64_t(M);
+        T1 += uint64_t(high);
+        R -= high ? int64_t(M) : 0;
+    }
+    int bexp = 2045 - E;
+    uint64_t out;
+    if (bexp >= 1) {
+        uint64_t Q = T1 + uint64_t(2 * uint64_t(R) > M);
+        const bool carry = (Q >> 53) != 0;
+        Q = carry ? Q >> 1 : Q;
+        bexp += int(carry);
+        out = sign | (uint64_t(bexp) << 52) | (Q & 0xfffffffffffffull);
+    } else {
+        const int k = 1 - bexp < 63 ? 1 - bexp : 63;
+        const uint64_t mant = T1 >> k;
+        const uint64_t dropped = T1 & ((1ull << k) - 1), half = 1ull << (k - 1);
+        const bool up = dropped > half || (dropped == half && (R > 0 || (mant & 1)));
+        out = sign | (mant + uint64_t(up));
+    }
+    return double_of(out);
 }
 
 }  // namespace dm

@@ -1620,7 +1620,9 @@ template<int H> struct AugLayout {
     static constexpr int kStrands = 32 / kLanes;     // strands per warp
 };
 
-template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, uint32_t g, uint32_t first = 0)
+// Group g of the strands in solve order [first, end) (end 0: to the last).
+template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, uint32_t g, uint32_t first = 0,
+                                                                uint32_t end = 0)
 {
     using L = AugLayout<H>;
     const unsigned FULL = 0xffffffffu;
@@ -1629,7 +1631,7 @@ template<int H> __device__ __forceinline__ void solve_group_aug(const View &d, u
     const int base = grp * L::kLanes;
     const int c0 = h * L::kCols;  // first column of this lane
     const uint32_t k = first + g * L::kStrands + uint32_t(grp);
-    const bool member = grp < L::kStrands && k < d.S;
+    const bool member = grp < L::kStrands && k < (end ? end : d.S);
     uint32_t begin = 0, len = 0;
     if (member) {
         const uint32_t s = d.sorder[k];
@@ -2066,6 +2068,266 @@ __global__ void __launch_bounds__(128) k_block_solve_pairs(View d, uint32_t long
         }
         if (g >= items) break;
         solve_group_aug<1>(d, g - long_strands, long_strands);
+    }
+}
+
+// ---- long strands on four warps ------------------------------------------
+//
+// One warp issues at most one FP64 instruction per ~64 cycles, so a strand
+// is bound by the FP64 instructions its busiest warp issues per node (about
+// 84 with 18 lanes, 45 on the pair's pivot warp, plus its reciprocals).  A
+// quad spreads a strand over the four warps of a block (four sub-partitions):
+// * the pivot warp (warp 0) holds B_n in the 18-lane layout, adds the shift
+//   and runs the six pivot steps; the reciprocal of every candidate of the
+//   step's column is taken on the integer pipes (dm::recip_rn, equal to the
+//   FP64 division) while the pivot search runs, so the step's FP64 work is
+//   one product and the update of the remaining columns;
+// * column warps 1-3 hold columns 2(w-1), 2(w-1)+1 of [U_n], one entry per
+//   lane (slots 0-11), and the right-hand side (slots 12-17, used in warp
+//   3); they apply each published step one behind, scale the rows, store
+//   C_n and d'_n, and form their two columns of the next Schur complement
+//   B_{n+1} = D_{n+1} - U_n^T C_n (column c of B needs column c of C only)
+//   and, in warp 3, the next right-hand side; warp 1 then runs the back
+//   substitution.
+// Each entry goes through the same operations in the same order as in
+// solve_group_aug<3>, so the directions are identical bit for bit.  The four
+// warps meet at a named barrier (128 threads) once per pivot step and once
+// per node; all execute the same number by construction (same strand, six
+// steps per node, no early exit).  Lanes 18-31 shadow lanes 0-13 (full-warp
+// shuffles; they write nothing).
+struct QuadShared {
+    double B[36];      // B_n, row-major, from the column warps to the pivot warp
+    double fp[2][6];   // row factors of a step (double-buffered by step parity)
+    double ip[2];      // the step's pivot reciprocal
+    int pivot[2];      // the step's pivot row
+    int ok[2];         // no pivot failure in this node up to and including the step
+    uint32_t item[2];  // work item (double-buffered by fetch parity)
+};
+
+__device__ __forceinline__ void quad_barrier(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+
+__device__ void solve_quad_pivot(const View &d, uint32_t k, QuadShared &sh, int bar)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gl = lane < 18 ? lane : lane - 18;
+    const int r = gl % 6, h = gl / 6, c0 = 2 * h;
+    uint32_t begin, len;
+    pair_strand_range(d, k, begin, len);
+    for (uint32_t t = 0; t < len; ++t) {
+        quad_barrier(bar);  // B_t is in shared memory
+        double a[2] = {sh.B[6 * r + c0], sh.B[6 * r + c0 + 1]};
+        double diag_r = 0.0;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) if (c0 + j == r) diag_r = a[j];
+        unsigned long long smax = 0ull;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(__shfl_sync(FULL, diag_r, 6 * (q / 2) + q)) &
+                                         0x7fffffffffffffffull;
+            smax = b > smax ? b : smax;
+        }
+        const double shift = fmax(__dmul_rn(1.0e-12, __longlong_as_double((long long)smax)), 1.0e-24);
+#pragma unroll
+        for (int j = 0; j < 2; ++j) if (c0 + j == r) a[j] = __dadd_rn(a[j], shift);
+        bool ok = true;
+#pragma unroll
+        for (int col = 0; col < 6; ++col) {
+            const int hc = col / 2, jc = col % 2, owner_half = 6 * hc;
+            double acol = 0.0;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) if (j == jc && h == hc) acol = a[j];
+            // Every candidate's reciprocal, alongside the pivot search; the
+            // pivot's is the one the 18-lane layout takes after the swap.
+            const double rc = dm::recip_rn(acol);
+            const unsigned long long mb = (unsigned long long)__double_as_longlong(acol) & 0x7fffffffffffffffull;
+            int pivot = col;
+            unsigned long long best = __shfl_sync(FULL, mb, owner_half + col);
+#pragma unroll
+            for (int row = col + 1; row < 6; ++row) {
+                const unsigned long long vrow = __shfl_sync(FULL, mb, owner_half + row);
+                if (vrow > best) { best = vrow; pivot = row; }
+            }
+            if (best < 0x39b4484bfeebc2a0ull || best >= 0x7ff0000000000000ull) ok = false;
+            const double ip = __shfl_sync(FULL, rc, owner_half + pivot);
+            const int partner = r == col ? pivot : (r == pivot ? col : r);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) a[j] = __shfl_sync(FULL, a[j], 6 * h + partner);
+            acol = 0.0;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) if (j == jc && h == hc) acol = a[j];
+            const double fp = __dmul_rn(__shfl_sync(FULL, acol, owner_half + r), ip);
+            const int prow = 6 * h + col;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                if (2 * 2 + j <= col) continue;  // finished in every lane
+                const double x = __shfl_sync(FULL, a[j], prow);
+                a[j] = (r == col) ? a[j] : __fma_rn(-fp, x, a[j]);
+            }
+            const int slot = col & 1;
+            if (lane < 6) sh.fp[slot][lane] = fp;
+            if (lane == 0) {
+                sh.ip[slot] = ip;
+                sh.pivot[slot] = pivot;
+                sh.ok[slot] = ok ? 1 : 0;
+            }
+            quad_barrier(bar);  // step published
+        }
+    }
+}
+
+__device__ void solve_quad_columns(const View &d, uint32_t k, QuadShared &sh, int bar, int w)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int s = lane < 18 ? lane : lane - 18;
+    const int r = s % 6, jj = s / 6;                 // jj 0, 1: a column of U; 2: the right-hand side
+    const int c = 2 * (w - 1) + (jj < 2 ? jj : 0);
+    const bool writer = lane < 18;
+    uint32_t begin, len;
+    pair_strand_range(d, k, begin, len);
+    double nd = 0.0, nu = 0.0, nuc[6], ng = 0.0;
+    auto fetch = [&](uint32_t t) {
+        const bool on = t < len;
+        const size_t n = begin + t;
+        nd = on ? d.diag[36 * n + 6 * r + c] : 0.0;
+        ng = on ? d.grad[6 * n + r] : 0.0;
+        nu = (on && t + 1 < len) ? d.upper[36 * n + 6 * r + c] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) nuc[q] = (on && t > 0) ? d.upper[36 * (n - 1) + 6 * q + r] : 0.0;
+    };
+    fetch(0);
+    double prev = 0.0;  // C_{t-1}[r][c] or d'_{t-1}[r]
+    bool failed = false;
+    for (uint32_t t = 0; t < len; ++t) {
+        const bool on = !failed;
+        const size_t n = begin + t;
+        double acc = jj < 2 ? nd : -ng, ucol[6];
+        const double u_next = nu;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) ucol[q] = nuc[q];
+        if (t + 1 < len) fetch(t + 1);
+        if (t > 0) {
+            // B = D - U_{t-1}^T C_{t-1} (column c), rhs = -g - U_{t-1}^T d'_{t-1}
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                acc = __fma_rn(-ucol[q], __shfl_sync(FULL, prev, 6 * jj + q), acc);
+            }
+        }
+        if (writer && jj < 2) sh.B[6 * r + c] = acc;
+        double v = jj < 2 ? u_next : acc;
+        quad_barrier(bar);  // hand B_t over
+        double ipiv = 1.0;
+        bool ok = true;
+#pragma unroll
+        for (int col = 0; col < 6; ++col) {
+            quad_barrier(bar);  // step published
+            const int slot = col & 1;
+            const int pivot = sh.pivot[slot];
+            const double fp = sh.fp[slot][r], ip = sh.ip[slot];
+            ok = sh.ok[slot] != 0;
+            const int partner = r == col ? pivot : (r == pivot ? col : r);
+            v = __shfl_sync(FULL, v, 6 * jj + partner);
+            if (r == col) ipiv = ip;
+            const double x = __shfl_sync(FULL, v, 6 * jj + col);
+            v = (r == col) ? v : __fma_rn(-fp, x, v);
+        }
+        v = __dmul_rn(v, ipiv);
+        if (on && !ok) {
+            failed = true;
+            if (w == 1 && lane == 0) atomicExch(&d.sc->solve_failed, 1);
+        }
+        prev = v;
+        if (on && !failed && writer) {
+            if (jj < 2) d.cprime[36 * n + 6 * r + c] = v;
+            else if (w == 3) d.dprime[6 * n + r] = v;
+        }
+    }
+    // Back substitution d_n = d'_n - C_n d_{n+1} in warp 1, once the three
+    // column warps have stored C and d' (barrier bar + 1, 96 threads).
+    asm volatile("bar.sync %0, 96;" ::"r"(bar + 1) : "memory");
+    if (w != 1) return;
+    double next = 0.0, pc[6], pd = 0.0;
+    auto fetch_back = [&](uint32_t t) {
+        const bool on = t < len && !failed;
+        const size_t n = begin + t;
+        pd = on ? d.dprime[6 * n + r] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) pc[q] = on ? d.cprime[36 * n + 6 * r + q] : 0.0;
+    };
+    if (len) fetch_back(len - 1);
+    for (uint32_t t = len; t-- > 0;) {
+        const bool on = !failed;
+        const size_t n = begin + t;
+        double value = pd, crow[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) crow[q] = pc[q];
+        if (t > 0) fetch_back(t - 1);
+        const bool coupled = on && t + 1 < len;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const double dq = __shfl_sync(FULL, next, q);
+            if (coupled) value = __fma_rn(-crow[q], dq, value);
+        }
+        if (on && lane < 6) d.dir[6 * n + r] = value;
+        next = on ? value : 0.0;
+    }
+}
+
+// Tiered schedule over one longest-first queue: the `quads` longest strands
+// on a block of four warps each, the next `singles` one per warp (18 lanes),
+// the next `doubles` two per warp (12 lanes each), the rest five per warp.
+// A block takes queue items together while they are quads; at the first
+// item past them its warps go on alone.  Every tier computes each entry
+// with the same operations, so the split changes no result.
+// The tiers are inlined: as separate functions they would take the View by
+// reference, which places the kernel's parameter block in local memory.
+__device__ __forceinline__ void tier_quad(const View &d, uint32_t g, QuadShared &sh, int warp)
+{
+    if (warp == 0) solve_quad_pivot(d, g, sh, 1);
+    else solve_quad_columns(d, g, sh, 1, warp);
+}
+__device__ __forceinline__ void tier_single(const View &d, uint32_t g, uint32_t first) { solve_group_aug<3>(d, g, first); }
+__device__ __forceinline__ void tier_double(const View &d, uint32_t g, uint32_t first, uint32_t end)
+{
+    solve_group_aug<2>(d, g, first, end);
+}
+__device__ __forceinline__ void tier_five(const View &d, uint32_t g, uint32_t first) { solve_group_aug<1>(d, g, first); }
+
+__global__ void __launch_bounds__(128) k_block_solve_tiers(View d, uint32_t quads, uint32_t singles, uint32_t doubles)
+{
+    __shared__ QuadShared sh;
+    const int warp = threadIdx.x >> 5;
+    const uint32_t end1 = quads + singles, end2 = end1 + doubles;
+    const uint32_t i2 = end1 + (doubles + 1) / 2;  // first five-strand item
+    const uint32_t rest = d.S > end2 ? d.S - end2 : 0;
+    const uint32_t items = i2 + (rest + AugLayout<1>::kStrands - 1) / AugLayout<1>::kStrands;
+    bool together = quads > 0;
+    uint32_t parity = 0;
+    for (;;) {
+        uint32_t g = 0;
+        if (together) {
+            if (threadIdx.x == 0) sh.item[parity] = atomicAdd(&d.sc->solve_next, 1u);
+            quad_barrier(1);
+            g = sh.item[parity];
+            parity ^= 1u;
+            if (g < quads) {
+                tier_quad(d, g, sh, warp);
+                continue;
+            }
+            together = false;  // every later item is a one-warp item
+            if (warp != 0) {
+                if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+                g = __shfl_sync(0xffffffffu, g, 0);
+            }
+        } else {
+            if ((threadIdx.x & 31) == 0) g = atomicAdd(&d.sc->solve_next, 1u);
+            g = __shfl_sync(0xffffffffu, g, 0);
+        }
+        if (g >= items) break;
+        if (g < end1) tier_single(d, g - quads, quads);
+        else if (g < i2) tier_double(d, g - end1, end1, end2);
+        else tier_five(d, g - i2, end2);
     }
 }
 
@@ -2923,6 +3185,8 @@ struct Engine::Impl {
     void (*solve_kernel)(View) = nullptr;
     uint32_t solve_long = 0;  // > 0: k_block_solve_hybrid / k_block_solve_pairs with this many long strands
     bool solve_pairs = false; // the long strands on warp pairs (k_block_solve_pairs)
+    bool solve_tiers = false; // k_block_solve_tiers with tier_quads / tier_singles / tier_doubles
+    uint32_t tier_quads = 0, tier_singles = 0, tier_doubles = 0;
     std::vector<uint32_t> sorted_len;  // free nodes per strand, in the solve order
     unsigned ff_blocks = 0;     // launch shape of the float-float kernels
     std::vector<KernelStat> kstats;
@@ -3468,7 +3732,7 @@ KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t b
 {
     Impl &I = *d_;
     if (strands_per_warp == 0) {
-        I.solve_blocks = 0; I.solve_kernel = nullptr; I.solve_long = 0; I.solve_pairs = false;
+        I.solve_blocks = 0; I.solve_kernel = nullptr; I.solve_long = 0; I.solve_pairs = false; I.solve_tiers = false;
         return KHS_OK;
     }
     if ((strands_per_warp != 5 && strands_per_warp != 2 && strands_per_warp != 1) || blocks_per_sm < 1 || blocks_per_sm > 8 ||
@@ -3484,7 +3748,39 @@ KhsResult Engine::set_block_solve_schedule(uint32_t strands_per_warp, uint32_t b
                                              : k_block_solve_aug<3>;
     I.solve_long = long_strands;
     I.solve_pairs = long_strands && strands_per_warp == 1;
+    I.solve_tiers = false;
     I.solve_blocks = std::min(std::max(1u, (groups + 3) / 4), blocks_per_sm * unsigned(sms));
+    const unsigned ff_groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
+    I.ff_blocks = std::min(std::max(1u, (ff_groups + 3) / 4), 2u * unsigned(sms));
+    return KHS_OK;
+}
+
+// Queue items of the tiered schedule: one per quad strand and per single,
+// one per two doubles, one per five of the rest.
+static unsigned tier_items(uint32_t S, uint32_t quads, uint32_t singles, uint32_t doubles)
+{
+    const uint32_t head = quads + singles + doubles;
+    return quads + singles + (doubles + 1) / 2 + (S > head ? (S - head + 4) / 5 : 0);
+}
+
+// Tiered launch shape (k_block_solve_tiers): the `quads` longest strands on
+// four warps each, the next `singles` on one warp of 18 lanes, the next
+// `doubles` two per warp, the rest five per warp; blocks_per_sm 1-8.  The
+// shape does not change the result.
+KhsResult Engine::set_block_solve_tiers(uint32_t quads, uint32_t singles, uint32_t doubles, uint32_t blocks_per_sm)
+{
+    Impl &I = *d_;
+    if (blocks_per_sm < 1 || blocks_per_sm > 8 || uint64_t(quads) + singles + doubles > I.v.S)
+        return KHS_ERROR_INVALID_ARGUMENT;
+    int sms = 0;
+    KHS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, kDevice));
+    I.solve_kernel = nullptr;
+    I.solve_long = 0;
+    I.solve_pairs = false;
+    I.solve_tiers = true;
+    I.tier_quads = quads; I.tier_singles = singles; I.tier_doubles = doubles;
+    const unsigned items = tier_items(I.v.S, quads, singles, doubles);
+    I.solve_blocks = std::min(std::max(1u, (items + 3) / 4), blocks_per_sm * unsigned(sms));
     const unsigned ff_groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
     I.ff_blocks = std::min(std::max(1u, (ff_groups + 3) / 4), 2u * unsigned(sms));
     return KHS_OK;
@@ -3498,12 +3794,14 @@ void Engine::tune_block_solve()
     cudaEvent_t ev[2];
     KHS_CUDA(cudaEventCreate(&ev[0]));
     KHS_CUDA(cudaEventCreate(&ev[1]));
-    auto time_it = [&](void (*kernel)(View), unsigned blocks, uint32_t nlong, bool pairs = false) {
+    auto time_it = [&](void (*kernel)(View), unsigned blocks, uint32_t nlong, bool pairs = false,
+                       const uint32_t *tiers = nullptr) {
         float best = 3.0e38f;
         for (int rep = 0; rep < 2; ++rep) {
             KHS_CUDA(cudaMemsetAsync(&I.v.sc->solve_next, 0, sizeof(uint32_t), I.stream));
             KHS_CUDA(cudaEventRecord(ev[0], I.stream));
-            if (kernel) kernel<<<blocks, 128, 0, I.stream>>>(I.v);
+            if (tiers) k_block_solve_tiers<<<blocks, 128, 0, I.stream>>>(I.v, tiers[0], tiers[1], tiers[2]);
+            else if (kernel) kernel<<<blocks, 128, 0, I.stream>>>(I.v);
             else if (pairs) k_block_solve_pairs<<<blocks, 128, 0, I.stream>>>(I.v, nlong);
             else k_block_solve_hybrid<<<blocks, 128, 0, I.stream>>>(I.v, nlong);
             ++I.launches;
@@ -3526,6 +3824,7 @@ void Engine::tune_block_solve()
             const float ms = time_it(c.kernel, blocks, 0);
             if (ms < best_ms) {
                 best_ms = ms; I.solve_kernel = c.kernel; I.solve_blocks = blocks; I.solve_long = 0; I.solve_pairs = false;
+                I.solve_tiers = false;
             }
             if (blocks == most) break;
         }
@@ -3546,11 +3845,30 @@ void Engine::tune_block_solve()
                 const float ms = time_it(nullptr, blocks, nlong, pairs);
                 if (ms < best_ms) {
                     best_ms = ms; I.solve_kernel = nullptr; I.solve_blocks = blocks; I.solve_long = nlong; I.solve_pairs = pairs;
+                    I.solve_tiers = false;
                 }
             }
             if (blocks == most) break;
         }
     }
+    // Tiered: quads for the longest ~0.5-2% of the strands, then singles,
+    // doubles and five per warp, two blocks per SM (its 255 registers per
+    // thread leave no room for a third).
+    for (uint32_t qd : {110u, 75u, 55u})
+        for (uint32_t sd : {70u, 35u, 25u})
+            for (uint32_t dd : {34u, 17u}) {
+                const uint32_t tiers[3] = {I.v.S / qd, I.v.S / sd, (I.v.S / dd) & ~1u};
+                if (tiers[0] == 0 || uint64_t(tiers[0]) + tiers[1] + tiers[2] >= I.v.S) continue;
+                const unsigned items = tier_items(I.v.S, tiers[0], tiers[1], tiers[2]);
+                const unsigned most = std::max(1u, (items + 3) / 4);
+                const unsigned blocks = std::min(most, 2u * unsigned(sms));
+                const float ms = time_it(nullptr, blocks, 0, false, tiers);
+                if (ms < best_ms) {
+                    best_ms = ms; I.solve_kernel = nullptr; I.solve_blocks = blocks; I.solve_long = 0;
+                    I.solve_pairs = false; I.solve_tiers = true;
+                    I.tier_quads = tiers[0]; I.tier_singles = tiers[1]; I.tier_doubles = tiers[2];
+                }
+            }
     // Float-float kernels (5 strands of 6 lanes per warp).
     {
         const unsigned groups = unsigned((I.v.S + kSolveGroupsPerWarp - 1) / kSolveGroupsPerWarp);
@@ -3566,6 +3884,9 @@ void Engine::launch_block_solve()
 {
     Impl &I = *d_;
     if (I.solve_kernel) I.launch("k_block_solve", I.solve_kernel, I.solve_blocks, 128, I.v);
+    else if (I.solve_tiers)
+        I.launch("k_block_solve", k_block_solve_tiers, I.solve_blocks, 128, I.v, I.tier_quads, I.tier_singles,
+                 I.tier_doubles);
     else if (I.solve_pairs) I.launch("k_block_solve", k_block_solve_pairs, I.solve_blocks, 128, I.v, I.solve_long);
     else I.launch("k_block_solve", k_block_solve_hybrid, I.solve_blocks, 128, I.v, I.solve_long);
 }

@@ -92,6 +92,7 @@ public:
     // warps per SM (long_strands > 0 with 5: the longest strands one per
     // warp first); 0 strands per warp restores the one-time tuning.
     KhsResult set_block_solve_schedule(uint32_t strands_per_warp, uint32_t blocks_per_sm, uint32_t long_strands);
+    KhsResult set_block_solve_tiers(uint32_t quads, uint32_t singles, uint32_t doubles, uint32_t blocks_per_sm);
     uint32_t mode() const { return mode_; }
 
     KhsStepStats stats() const { return step_stats_; }

@@ -207,6 +207,7 @@ EXTENSION_FUNCTIONS = [
     ("khsxCopyContactRecords", ctypes.c_int, [VP, VP, c_u32]),
     ("khsxQueryContacts", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
     ("khsxSetBlockSolveSchedule", ctypes.c_int, [VP, c_u32, c_u32, c_u32]),
+    ("khsxSetBlockSolveTiers", ctypes.c_int, [VP, c_u32, c_u32, c_u32, c_u32]),
     ("khsxSetRollbackRing", ctypes.c_int, [VP, c_u32]),
     ("khsxRollbackToFrame", ctypes.c_int, [VP, c_u32]),
     ("khsxQueryContactsNoAlloc", ctypes.c_int, [VP, VP, c_u64, VP, c_u32]),
@@ -223,7 +224,7 @@ EXTENSION_FUNCTIONS = [
 
 # Entry points the CPU oracle does not provide (device-only measurement).
 DEVICE_ONLY = {"khsxSetProfiling", "khsxGetKernelTimings", "khsxResetKernelTimings", "khsxGetKernelLaunchCount",
-               "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc", "khsxSetBlockSolveSchedule",
+               "khsxMeasurePipePeaks", "khsxQueryContactsNoAlloc", "khsxSetBlockSolveSchedule", "khsxSetBlockSolveTiers",
                "khsxSetRollbackRing", "khsxRollbackToFrame", "khsxSetOutputRing", "khsxCopyOutputFrame",
                "khsxMapOutputFrame"}
 
@@ -501,6 +502,9 @@ class HairSolver:
 
     def set_block_solve_schedule(self, strands_per_warp: int, blocks_per_sm: int = 1, long_strands: int = 0) -> None:
         self._check(self._library.khsxSetBlockSolveSchedule(self._handle, strands_per_warp, blocks_per_sm, long_strands))
+
+    def set_block_solve_tiers(self, quads: int, singles: int, doubles: int, blocks_per_sm: int = 2) -> None:
+        self._check(self._library.khsxSetBlockSolveTiers(self._handle, quads, singles, doubles, blocks_per_sm))
 
     def query_contacts_no_alloc(self, q: np.ndarray, out: np.ndarray) -> int:
         """khsxQueryContactsNoAlloc into a caller-owned CONTACT_DTYPE array;

@@ -198,3 +198,31 @@ def test_block_solve_layouts_bit_identical(gpu_lib):
         s.close()
     for q, v in finals[1:]:
         assert np.array_equal(q, finals[0][0]) and np.array_equal(v, finals[0][1])
+
+
+def test_block_solve_tiers_bit_identical(gpu_lib):
+    """The tiered shapes (the longest strands on four warps each, then one
+    and two per warp, the rest five per warp; odd pair counts, every strand
+    on four warps, 1-3 blocks per SM) give the same trajectory bit for bit
+    as the five-per-warp layout, and the tuned shape does too."""
+    sc = scenes.ellipsoid_scene(strands=200, frames=2)
+    shapes = [None, "tuned", (10, 20, 41, 2), (37, 0, 0, 3), (1, 1, 1, 1), (200, 0, 0, 2), (0, 60, 60, 2), (25, 25, 150, 3)]
+    finals = []
+    for shape in shapes:
+        s = kn.HairSolver(gpu_lib)
+        scenes.load_into(s, sc)
+        if shape is None:
+            s.set_block_solve_schedule(5, 1, 0)
+        elif shape != "tuned":
+            s.set_block_solve_tiers(*shape)
+        for f in range(1, sc.frames):
+            assert s._library.khsStepAnimationFrame(s.handle, f, sc.frame_dt) == kn.OK, s.last_error()
+        finals.append(s.state())
+        s.close()
+    for shape, (q, v) in zip(shapes[1:], finals[1:]):
+        assert np.array_equal(q, finals[0][0]) and np.array_equal(v, finals[0][1]), shape
+    s = kn.HairSolver(gpu_lib)
+    scenes.load_into(s, sc)
+    assert s._library.khsxSetBlockSolveTiers(s.handle, 150, 40, 20, 2) == kn.ERROR_INVALID_ARGUMENT  # > strands
+    assert s._library.khsxSetBlockSolveTiers(s.handle, 1, 1, 1, 0) == kn.ERROR_INVALID_ARGUMENT
+    s.close()
