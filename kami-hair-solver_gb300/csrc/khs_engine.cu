@@ -3977,6 +3977,15 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
         ++step_stats_.linear_solves;
         KHS_CUDA(cudaMemcpyAsync(v.q_base, v.q, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
         bool accepted = false;
+        // The first trial of the Gauss-Newton direction also evaluates the
+        // gradient, the Hessian blocks and the rotation Jacobians (its
+        // energy is computed by the same operations as an energy-only
+        // evaluation).  When it is accepted -- most iterations -- that
+        // evaluation is the next iterate's, and the separate evaluation at
+        // the accepted state is skipped: same values, one evaluation fewer.
+        bool graded_trial = false;     // a trial evaluated the gradient at its own state
+        bool accepted_graded = false;  // ... and it was the accepted one
+        EvalStats graded{};
         double alpha = 1.0;
         for (int attempt = 0; attempt < 2; ++attempt) {
             // Slope of the (possibly scaled) direction, and the CCD bound.
@@ -4015,12 +4024,16 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
             progress_phase_.store(KHS_PHASE_LINE_SEARCH);
             if (alpha >= desc_.minimum_line_search_step)
                 for (uint32_t s = 0; s < desc_.line_search_iterations; ++s) {
-                    const EvalStats trial = evaluate(false, dt, alpha);
+                    const bool with_gradient = attempt == 0 && s == 0;
+                    const EvalStats trial = evaluate(with_gradient, dt, alpha);
+                    graded_trial = graded_trial || with_gradient;
                     ++step_stats_.line_search_evaluations;
                     ++rec.line_search_evaluations;
                     if (trial.feasible && std::isfinite(trial.objective) &&
                         trial.objective <= current.objective + 1e-4 * alpha * slope) {
                         accepted = true;
+                        accepted_graded = with_gradient;
+                        if (with_gradient) graded = trial;
                         break;
                     }
                     alpha *= 0.5;
@@ -4029,6 +4042,10 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
             if (accepted) break;
             if (!block_direction) break;
             KHS_CUDA(cudaMemcpyAsync(v.q, v.q_base, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+            // The trials left their own gradient, blocks, rotations and FP32
+            // positions behind; the steepest direction (gradient) and the
+            // mixed form's CCD filter (FP32 positions) need the iterate's.
+            if (graded_trial) evaluate(true, dt, -1.0);
             ++rec.steepest_fallbacks;
             if (make_steepest()) ++rec.trust_scalings;
             block_direction = false;
@@ -4038,7 +4055,7 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
             I.sync();
             return fail(KHS_ERROR_NOT_CONVERGED, "Gauss-Newton line search failed");
         }
-        current = evaluate(true, dt, -1.0);
+        current = accepted_graded ? graded : evaluate(true, dt, -1.0);
         const double dnorm = std::sqrt(I.mail_host->dir_norm2);
         step_stats_.increment_norm = alpha * dnorm;
         step_stats_.accepted_step_length = alpha;
