@@ -241,6 +241,14 @@ def _ptr(array: np.ndarray | None):
     return None if array is None else ctypes.c_void_p(array.ctypes.data)
 
 
+class KhsError(RuntimeError):
+    """A failed C-ABI call: ``code`` is its KhsResult."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = int(code)
+
+
 class Library:
     """Loaded ABI library with typed entry points (raw result codes)."""
 
@@ -323,7 +331,7 @@ class HairSolver:
 
     def _check(self, result: int):
         if result != OK:
-            raise RuntimeError(self.last_error() or f"hair solver error {result}")
+            raise KhsError(result, self.last_error() or f"hair solver error {result}")
 
     # -- scene input ------------------------------------------------------
     def set_hair(self, points, offsets):

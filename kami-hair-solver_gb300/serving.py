@@ -121,7 +121,7 @@ def run_request(lib, req: Request, mode: int, ring_slots: int, on_resident=None)
             res.substeps.append(int(s.stats().substeps))
         res.q = s.state()[0]
     except Exception as exc:  # a failed request must not stop the server
-        res.status, res.error = kn.ERROR_INTERNAL, str(exc)
+        res.status, res.error = getattr(exc, "code", kn.ERROR_INTERNAL), str(exc)
     finally:
         s.close()
     return res
@@ -228,6 +228,10 @@ def run_serial(lib, requests: list[Request], mode: int, ring_slots: int = 0) -> 
 
 def summary(results: list[Result], makespan: float) -> dict:
     lat = [ms for r in results for ms in r.frame_ms]
+    failed = {}
+    for r in results:
+        if r.status != kn.OK:
+            failed[str(r.status)] = failed.get(str(r.status), 0) + 1
     node_substeps = sum(r.nodes * sum(r.substeps) for r in results)
     ok = [r for r in results if r.status == kn.OK]
     return {
@@ -238,6 +242,7 @@ def summary(results: list[Result], makespan: float) -> dict:
         "node_substeps_per_s": node_substeps / makespan if makespan > 0 else None,
         "makespan_s": makespan,
         "mean_queue_s": statistics.fmean(r.admitted - r.arrival for r in results) if results else None,
+        "failed_by_result": failed,
         "reserved_bytes_total": sum(r.bytes for r in results),
         "resident_bytes_total": sum(r.resident for r in results),
     }
@@ -303,8 +308,9 @@ def main() -> None:
         pres, span = run_serial(lib, sample, kn.MODE_PLAIN_FP64, args.ring)
         line["sample"] = {"requests": len(sample), "mixed_batched": summary(sres, sserver.makespan),
                           "plain_serial": summary(pres, span),
-                          "same_final_state": all(a.q is not None and b.q is not None and (a.q == b.q).all()
-                                                  for a, b in zip(sres, pres))}
+                          "same_status": all(a.status == b.status for a, b in zip(sres, pres)),
+                          "same_final_state": all((a.q == b.q).all() for a, b in zip(sres, pres)
+                                                  if a.status == kn.OK and b.status == kn.OK)}
     print(json.dumps(line), flush=True)
 
 

@@ -79,3 +79,22 @@ def test_reported_bytes_above_the_estimate_hold_back_admission():
     res = server.run(reqs)
     assert all(r.status == kn.OK for r in res)
     assert len(res) == 3 and server.peak_slots <= 2
+
+
+def test_rejected_request_reports_the_solver_result(oracle_lib):
+    """A request whose hair starts inside the closed collider is rejected by
+    khsBuild with KHS_ERROR_INITIAL_INTERSECTION, and the serving loop
+    reports that code (not a generic internal error); the other requests of
+    the stream complete."""
+    import numpy as np
+
+    good = scenes.sphere_scene(seed=3, strands=6, nodes=8, frames=2, motion=True)
+    bad = scenes.sphere_scene(seed=3, strands=6, nodes=8, frames=2, motion=True)
+    bad.points = np.asarray(bad.points) * 0.5  # every hair point inside the unit-radius sphere collider
+    bad.root_points_at = lambda f: bad.points
+    reqs = [serving.Request(rid=0, scene=good, arrival=0.0, frames=1), serving.Request(rid=1, scene=bad, arrival=0.0, frames=1)]
+    server = serving.Server(oracle_lib, 10 ** 12, max_slots=2, mode=kn.MODE_PLAIN_FP64, ring_slots=0)
+    res = server.run(reqs)
+    assert res[0].status == kn.OK
+    assert res[1].status == kn.ERROR_INITIAL_INTERSECTION, (res[1].status, res[1].error)
+    assert serving.summary(res, server.makespan)["failed_by_result"] == {str(kn.ERROR_INITIAL_INTERSECTION): 1}
