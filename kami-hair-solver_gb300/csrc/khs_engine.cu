@@ -85,6 +85,11 @@ struct Mailbox {
     uint32_t pair_count;
     uint32_t refine_bits;
     uint32_t pad;
+    // The direction pass's values (every k_final_dir but the CCD pass of a
+    // pipelined iteration, which reduces the already limited direction).
+    double dir_slope, dir_max_translation;
+    int dir_solve_failed;
+    int dir_pad;
 };
 
 // Atomic targets live in device memory; the publishing kernels copy them to
@@ -101,6 +106,8 @@ struct Scalars {
     uint32_t ccd_near;    // elements queued for the warp-cooperative CCD pass
     uint32_t eval_done;   // blocks of k_reduce_eval finished (the last one reduces the partials)
     uint32_t pool_used;   // entries of the leaf pool handed out since the last cache rebuild
+    double trial_alpha;   // first line-search step from the last CCD bound (k_final_dir)
+    double max_translation;  // largest free-node translation of the last reduced direction (k_final_dir)
 };
 
 struct Partial {
@@ -717,11 +724,11 @@ __global__ void __launch_bounds__(kBlock) k_precond(View d, double dt)
 // Per node: optional line-search update q = q_base + alpha dir, rotation
 // cache, inertia + damping energy, gradient and diagonal
 // (cuda_backend.cu:883-897).
-__global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int trial, double alpha, double dt)
+// Trial state q = q_base + alpha dir (trial) and the FP32 position copy.
+// alpha_dev (if set) holds the trial step in device memory (the pipelined
+// first trial of an iteration, whose step the host has not read yet).
+__device__ __forceinline__ void node_positions(const View &d, uint32_t n, int trial, double alpha, double q[6])
 {
-    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= d.N) return;
-    double q[6];
     const size_t o = 6 * size_t(n);
     if (trial) {
 #pragma unroll
@@ -731,6 +738,33 @@ __global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int 
         for (int k = 0; k < 6; ++k) q[k] = d.q[o + k];
     }
     d.q32[3 * size_t(n)] = float(q[0]); d.q32[3 * size_t(n) + 1] = float(q[1]); d.q32[3 * size_t(n) + 2] = float(q[2]);
+}
+
+// The positions alone, so that the contact passes (which read q and the
+// FP32 copy) can run beside the rest of k_node_eval.
+__global__ void __launch_bounds__(kBlock) k_positions(View d, int trial, double alpha, const double *alpha_dev)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    double q[6];
+    node_positions(d, n, trial, alpha_dev ? *alpha_dev : alpha, q);
+}
+
+// positions_done: k_positions has written q and the FP32 copy.
+__global__ void __launch_bounds__(kBlock) k_node_eval(View d, int gradient, int trial, double alpha, double dt,
+                                                      const double *alpha_dev, int positions_done)
+{
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    if (alpha_dev) alpha = *alpha_dev;
+    double q[6];
+    const size_t o = 6 * size_t(n);
+    if (positions_done) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[k] = d.q[o + k];
+    } else {
+        node_positions(d, n, trial, alpha, q);
+    }
     M R, J;
     dm::rotation_and_jacobian(dm::v(q[3], q[4], q[5]), d.ref + 9 * size_t(n), R, gradient ? &J : nullptr);
 #pragma unroll
@@ -2678,6 +2712,16 @@ __global__ void __launch_bounds__(kBlock) k_scale(View d, double s)
     if (i < 6 * d.N) d.dir[i] *= s;
 }
 
+// The trust-radius limit applied on the device (pipelined iteration): the
+// same scale trust / max_translation as the host applies after reading the
+// reduction, when the direction's largest translation exceeds the radius.
+__global__ void __launch_bounds__(kBlock) k_scale_trust(View d, double trust)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double mt = d.sc->max_translation;
+    if (i < 6 * d.N && mt > trust) d.dir[i] *= trust / mt;
+}
+
 // g.d, |d|^2 and the largest free-node translation of d.
 __global__ void __launch_bounds__(kBlock) k_reduce_dir(View d)
 {
@@ -2705,7 +2749,9 @@ __global__ void __launch_bounds__(kBlock) k_reduce_dir(View d)
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_final_dir(View d)
+// ccd_pass: the CCD pass of a pipelined iteration, which leaves the
+// direction pass's values (dir_*) in the mailbox.
+__global__ void __launch_bounds__(kBlock) k_final_dir(View d, int ccd_pass)
 {
     __shared__ double sh2[2][kBlock];
     double gd = 0, dd = 0, mx = 0;
@@ -2719,8 +2765,16 @@ __global__ void __launch_bounds__(kBlock) k_final_dir(View d)
     gd = sums[0]; dd = sums[1]; mx = maxs[0];
     if (threadIdx.x == 0) {
         d.mail->slope = gd; d.mail->dir_norm2 = dd; d.mail->max_translation = mx;
+        d.sc->max_translation = mx;
         d.mail->ccd_bits = d.sc->ccd_bits;
         d.mail->solve_failed = d.sc->solve_failed;
+        if (!ccd_pass) {
+            d.mail->dir_slope = gd; d.mail->dir_max_translation = mx; d.mail->dir_solve_failed = d.sc->solve_failed;
+        }
+        // The first line-search step as the host forms it: 0.9 x the CCD
+        // bound below 1, else 1 (no collider: 1).
+        const double lim = __longlong_as_double((long long)d.sc->ccd_bits);
+        d.sc->trial_alpha = d.has_collider ? (lim < 1.0 ? __dmul_rn(lim, 0.9) : lim) : 1.0;
         d.mail->pair_count = d.sc->pair_count;
         d.mail->refine_bits = d.sc->refine_bits;
         d.sc->ccd_bits = 0x3ff0000000000000ULL;  // 1.0
@@ -3123,6 +3177,8 @@ struct Engine::Impl {
     View v{};
     Arena arena;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;          // contact passes beside the node kernel
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
     Mailbox *mail_host = nullptr;
     SweepRecord *sweep_host = nullptr;
@@ -3211,6 +3267,18 @@ struct Engine::Impl {
         kstats.push_back({name, 0, 0.0});
         return kstats.size() - 1;
     }
+    // A launch on stream s (the solver's stream, or the side stream, which
+    // is only used while kernels are not timed one by one).
+    template<class K, class... A> void launch_on(cudaStream_t s, const char *name, K kernel, unsigned grid, unsigned block,
+                                                 A... args)
+    {
+        if (s == stream) {
+            launch(name, kernel, grid, block, args...);
+            return;
+        }
+        ++launches;
+        kernel<<<grid, block, 0, s>>>(args...);
+    }
     template<class K, class... A> void launch(const char *name, K kernel, unsigned grid, unsigned block, A... args)
     {
         ++launches;
@@ -3251,6 +3319,9 @@ struct Engine::Impl {
         if (sweep_host) cudaFreeHost(sweep_host);
         if (ev_begin) cudaEventDestroy(ev_begin);
         if (ev_end) cudaEventDestroy(ev_end);
+        if (side) cudaStreamDestroy(side);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
         if (stream) cudaStreamDestroy(stream);
     }
     void sync()
@@ -3270,6 +3341,9 @@ void Engine::initialize(const Model &m, const KhsSolverDesc &desc, const KhsHair
     Impl &I = *d_;
     KHS_CUDA(cudaSetDevice(0));
     KHS_CUDA(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking));
+    KHS_CUDA(cudaStreamCreateWithFlags(&I.side, cudaStreamNonBlocking));
+    KHS_CUDA(cudaEventCreateWithFlags(&I.fork, cudaEventDisableTiming));
+    KHS_CUDA(cudaEventCreateWithFlags(&I.join, cudaEventDisableTiming));
     KHS_CUDA(cudaEventCreate(&I.ev_begin));
     KHS_CUDA(cudaEventCreate(&I.ev_end));
     KHS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&I.mail_host), sizeof(Mailbox), cudaHostAllocMapped));
@@ -3670,21 +3744,38 @@ KhsProgress Engine::progress() const
     return p;
 }
 
-EvalStats Engine::evaluate(bool gradient, double dt, double alpha)
+EvalStats Engine::evaluate(bool gradient, double dt, double alpha, const double *alpha_dev)
 {
     Impl &I = *d_;
     const View &v = I.v;
-    const bool trial = alpha >= 0.0;
-    I.launch(gradient ? "k_node_eval_grad" : "k_node_eval_energy", k_node_eval, grid_for(v.N), kBlock, v, gradient ? 1 : 0,
-             trial ? 1 : 0, trial ? alpha : 0.0, dt);
+    const bool trial = alpha >= 0.0 || alpha_dev;
+    const double a = alpha >= 0.0 ? alpha : 0.0;
     if (mode_ && v.has_collider) {
+        // The mixed form's contact passes read only q and its FP32 copy: once
+        // k_positions has written them, the passes run on a second stream
+        // beside the node kernel (on one stream while kernels are timed one by
+        // one).  The same kernels see the same inputs either way.
+        I.launch("k_positions", k_positions, grid_for(v.N), kBlock, v, trial ? 1 : 0, a, alpha_dev);
+        const bool side = !I.profiling;
+        const cudaStream_t cs = side ? I.side : I.stream;
+        if (side) {
+            KHS_CUDA(cudaEventRecord(I.fork, I.stream));
+            KHS_CUDA(cudaStreamWaitEvent(I.side, I.fork, 0));
+        }
         const double *q = v.q;
-        if (rebuild_cache_) KHS_CUDA(cudaMemsetAsync(&v.sc->pool_used, 0, sizeof(uint32_t), I.stream));
-        I.launch(rebuild_cache_ ? "k_contact_filter_rebuild" : trial ? "k_contact_filter_trial" : "k_contact_filter", k_contact_filter,
-                 grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
-        I.launch("k_contact_near", k_contact_near, 152 * 8, kBlock, v);
-        I.launch("k_contact_exact", k_contact_exact, 152 * 4, kBlock, v, q);
-        I.launch("k_contact_select", k_contact_select, grid_for(v.E), kBlock, v, q);
+        if (rebuild_cache_) KHS_CUDA(cudaMemsetAsync(&v.sc->pool_used, 0, sizeof(uint32_t), cs));
+        I.launch_on(cs, rebuild_cache_ ? "k_contact_filter_rebuild" : trial ? "k_contact_filter_trial" : "k_contact_filter",
+                    k_contact_filter, grid_for(v.E), kBlock, v, q, rebuild_cache_ ? 1 : 0);
+        I.launch_on(cs, "k_contact_near", k_contact_near, 152 * 8, kBlock, v);
+        I.launch_on(cs, "k_contact_exact", k_contact_exact, 152 * 4, kBlock, v, q);
+        I.launch_on(cs, "k_contact_select", k_contact_select, grid_for(v.E), kBlock, v, q);
+        if (side) KHS_CUDA(cudaEventRecord(I.join, I.side));
+        I.launch(gradient ? "k_node_eval_grad" : "k_node_eval_energy", k_node_eval, grid_for(v.N), kBlock, v,
+                 gradient ? 1 : 0, trial ? 1 : 0, a, dt, alpha_dev, 1);
+        if (side) KHS_CUDA(cudaStreamWaitEvent(I.stream, I.join, 0));
+    } else {
+        I.launch(gradient ? "k_node_eval_grad" : "k_node_eval_energy", k_node_eval, grid_for(v.N), kBlock, v,
+                 gradient ? 1 : 0, trial ? 1 : 0, a, dt, alpha_dev, 0);
     }
     rebuild_cache_ = false;
     I.launch(gradient ? "k_elem_eval_grad" : "k_elem_eval_energy", mode_ ? k_elem_eval<true> : k_elem_eval<false>, grid_for(v.E),
@@ -3716,7 +3807,7 @@ bool Engine::make_steepest()
     Impl &I = *d_;
     I.launch("k_steepest", k_steepest, grid_for(6 * size_t(I.v.N)), kBlock, I.v);
     I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
-    I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
+    I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v, 0);
     I.check();
     I.sync();
     return limit_direction(I.mail_host->max_translation);
@@ -3906,7 +3997,7 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
             I.launch("k_ff_correct", k_ff_correct, I.ff_blocks, 128, I.v);
             ++sweeps;
             I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
-            I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
+            I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v, 0);
             I.check();
             I.sync();
             if (mb.solve_failed) break;
@@ -3923,7 +4014,7 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
     if (fp64) {
         launch_block_solve();
         I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, I.v);
-        I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v);
+        I.launch("k_final_dir", k_final_dir, 1, kBlock, I.v, 0);
         I.check();
         I.sync();
     }
@@ -3935,6 +4026,21 @@ bool Engine::make_direction(KhsxSubstepRecord &rec, double grad_norm2)
     }
     if (limit_direction(mb.max_translation)) ++rec.trust_scalings;
     return true;
+}
+
+// The line-search CCD bound of the current direction (the mixed form's
+// FP32-filtered pair list, or the per-element FP64 kernel).
+void Engine::launch_ccd_bound()
+{
+    Impl &I = *d_;
+    const View &v = I.v;
+    if (mode_) {
+        I.launch("k_ccd_collect", k_ccd_collect, grid_for(v.E), kBlock, v);
+        I.launch("k_ccd_near", k_ccd_near, 152u * 8u, kBlock, v);
+        I.launch("k_ccd_pairs", k_ccd_pairs, 152u * 8u, kBlock, v);
+    } else {
+        I.launch("k_ccd", k_ccd<false>, grid_for(v.E), kBlock, v);
+    }
 }
 
 KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
@@ -3973,9 +4079,60 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
         }
         if (it == desc_.newton_iterations) break;
         progress_phase_.store(KHS_PHASE_LINEAR_SOLVE);
-        bool block_direction = make_direction(rec, current.grad_norm2);
+        // FP64 solve: the direction, its CCD bound and the first line-search
+        // trial (at the step k_final_dir leaves in device memory) are enqueued
+        // together, with one host synchronisation instead of three.  The
+        // device runs the same kernels in the same order as step by step.
+        // The trust-radius limit is applied on the device (k_scale_trust, the
+        // host's scale when it applies, else nothing).  When the direction is
+        // not used as is (steepest fallback, CCD work-list overflow, step
+        // below the minimum) the trial is discarded: the iterate is restored
+        // and evaluated again, and the iteration goes on step by step.
+        bool block_direction;
+        bool pipelined = false;
+        EvalStats first{};
+        double first_alpha = 1.0, first_slope = 0.0;
+        if (mode_ != KHSX_MODE_MIXED_FF) {
+            if (!I.solve_blocks) tune_block_solve();
+            launch_block_solve();
+            I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, v);
+            I.launch("k_final_dir", k_final_dir, 1, kBlock, v, 0);
+            I.launch("k_scale", k_scale_trust, grid_for(6 * size_t(v.N)), kBlock, v, trust_radius_);
+            KHS_CUDA(cudaMemcpyAsync(v.q_base, v.q, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+            I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, v);
+            if (v.has_collider) launch_ccd_bound();
+            I.launch("k_final_dir", k_final_dir, 1, kBlock, v, 1);
+            first = evaluate(true, dt, -1.0, &v.sc->trial_alpha);
+            const Mailbox &mb = *I.mail_host;
+            const bool used = !mb.dir_solve_failed && mb.dir_slope < 0 && std::isfinite(mb.dir_slope);
+            const double max_translation = mb.dir_max_translation;
+            first_slope = mb.slope;  // of the (possibly limited) direction, from the CCD pass
+            if (v.has_collider) {
+                unsigned long long bits = mb.ccd_bits;
+                double lim;
+                std::memcpy(&lim, &bits, sizeof(lim));
+                first_alpha = lim;
+                if (first_alpha < 1.0) first_alpha *= 0.9;
+            }
+            const bool overflow = mode_ && v.has_collider && mb.pair_count > v.pair_capacity;
+            // The direction was limited to the trust radius on the device.
+            const bool scaled = max_translation > trust_radius_;
+            pipelined = used && !overflow && first_alpha >= desc_.minimum_line_search_step;
+            block_direction = used;
+            if (used && scaled) ++rec.trust_scalings;
+            if (!pipelined) {
+                KHS_CUDA(cudaMemcpyAsync(v.q, v.q_base, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+                evaluate(true, dt, -1.0);
+                if (!used) {
+                    ++rec.steepest_fallbacks;
+                    if (make_steepest()) ++rec.trust_scalings;
+                }
+            }
+        } else {
+            block_direction = make_direction(rec, current.grad_norm2);
+            KHS_CUDA(cudaMemcpyAsync(v.q_base, v.q, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
+        }
         ++step_stats_.linear_solves;
-        KHS_CUDA(cudaMemcpyAsync(v.q_base, v.q, 6 * size_t(v.N) * 8, cudaMemcpyDeviceToDevice, I.stream));
         bool accepted = false;
         // The first trial of the Gauss-Newton direction also evaluates the
         // gradient, the Hessian blocks and the rotation Jacobians (its
@@ -3988,44 +4145,45 @@ KhsResult Engine::optimize_substep(double dt, KhsxSubstepRecord &rec)
         EvalStats graded{};
         double alpha = 1.0;
         for (int attempt = 0; attempt < 2; ++attempt) {
-            // Slope of the (possibly scaled) direction, and the CCD bound.
-            I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, v);
-            if (v.has_collider) {
-                progress_phase_.store(KHS_PHASE_CCD);
-                if (mode_) {
-                    I.launch("k_ccd_collect", k_ccd_collect, grid_for(v.E), kBlock, v);
-                    I.launch("k_ccd_near", k_ccd_near, 152u * 8u, kBlock, v);
-                    I.launch("k_ccd_pairs", k_ccd_pairs, 152u * 8u, kBlock, v);
-                } else {
-                    I.launch("k_ccd", k_ccd<false>, grid_for(v.E), kBlock, v);
+            const bool reuse = pipelined && attempt == 0;  // bound and first trial already evaluated
+            double slope;
+            if (reuse) {
+                slope = first_slope;
+                alpha = first_alpha;
+            } else {
+                // Slope of the (possibly scaled) direction, and the CCD bound.
+                I.launch("k_reduce_dir", k_reduce_dir, kPartials, kBlock, v);
+                if (v.has_collider) {
+                    progress_phase_.store(KHS_PHASE_CCD);
+                    launch_ccd_bound();
                 }
-            }
-            I.launch("k_final_dir", k_final_dir, 1, kBlock, v);
-            I.check();
-            I.sync();
-            if (mode_ && v.has_collider && I.mail_host->pair_count > v.pair_capacity) {
-                // Work list overflow: redo the bound with the per-element kernel.
-                I.launch("k_ccd", k_ccd<true>, grid_for(v.E), kBlock, v);
-                I.launch("k_final_dir", k_final_dir, 1, kBlock, v);
+                I.launch("k_final_dir", k_final_dir, 1, kBlock, v, 0);
                 I.check();
                 I.sync();
+                if (mode_ && v.has_collider && I.mail_host->pair_count > v.pair_capacity) {
+                    // Work list overflow: redo the bound with the per-element kernel.
+                    I.launch("k_ccd", k_ccd<true>, grid_for(v.E), kBlock, v);
+                    I.launch("k_final_dir", k_final_dir, 1, kBlock, v, 0);
+                    I.check();
+                    I.sync();
+                }
+                slope = I.mail_host->slope;
+                alpha = 1.0;
+                if (v.has_collider) {
+                    unsigned long long bits = I.mail_host->ccd_bits;
+                    double lim;
+                    std::memcpy(&lim, &bits, sizeof(lim));
+                    alpha = lim;
+                    if (alpha < 1.0) alpha *= 0.9;
+                }
             }
-            const double slope = I.mail_host->slope;
-            alpha = 1.0;
-            if (v.has_collider) {
-                unsigned long long bits = I.mail_host->ccd_bits;
-                double lim;
-                std::memcpy(&lim, &bits, sizeof(lim));
-                alpha = lim;
-                if (alpha < 1.0) alpha *= 0.9;
-                step_stats_.ccd_step_limit = std::fmin(step_stats_.ccd_step_limit, alpha);
-            }
+            if (v.has_collider) step_stats_.ccd_step_limit = std::fmin(step_stats_.ccd_step_limit, alpha);
             accepted = false;
             progress_phase_.store(KHS_PHASE_LINE_SEARCH);
             if (alpha >= desc_.minimum_line_search_step)
                 for (uint32_t s = 0; s < desc_.line_search_iterations; ++s) {
                     const bool with_gradient = attempt == 0 && s == 0;
-                    const EvalStats trial = evaluate(with_gradient, dt, alpha);
+                    const EvalStats trial = reuse && s == 0 ? first : evaluate(with_gradient, dt, alpha);
                     graded_trial = graded_trial || with_gradient;
                     ++step_stats_.line_search_evaluations;
                     ++rec.line_search_evaluations;

@@ -125,10 +125,11 @@ private:
                         const double *rot_b, const double *collider_a, const double *collider_b, uint32_t frame,
                         uint32_t frame_count);
     KhsResult optimize_substep(double dt, KhsxSubstepRecord &rec);
-    EvalStats evaluate(bool gradient, double dt, double alpha_for_trial);
+    EvalStats evaluate(bool gradient, double dt, double alpha_for_trial, const double *alpha_dev = nullptr);
     bool make_direction(KhsxSubstepRecord &rec, double grad_norm2);
     void tune_block_solve();
     void launch_block_solve();
+    void launch_ccd_bound();
     void push_ring(uint32_t frame);
     // Both return whether the trust radius scaled the direction.
     bool make_steepest();
