@@ -226,18 +226,24 @@ __device__ __forceinline__ M load9(const double *p)
 }
 __device__ __forceinline__ V tri_vertex(const View &d, uint32_t t, int c) { return load3(d.col_cur + 3 * size_t(d.tri[3 * t + c])); }
 
+// Next node of a stackless walk after skipping node i's subtree.  In the
+// preorder layout a node's escape index is the end of its subtree, so it is
+// always greater than i; anything else (a corrupted or uninitialised tree)
+// ends the walk instead of restarting it.
+__device__ __forceinline__ uint32_t escape_from(uint32_t i, uint32_t escape) { return escape > i ? escape : 0xffffffffu; }
+
 // Stackless BVH walk in the reference's visiting order.
 template<class F> __device__ void bvh_query(const View &d, V lo, V hi, double pad, F &&f)
 {
     uint32_t i = 0;
     while (i < d.B) {
         const V nl = load3(d.blo + 3 * size_t(i)), nh = load3(d.bhi + 3 * size_t(i));
-        if (!dm::boxes_overlap(lo, hi, nl, nh, pad)) { i = d.besc[i]; continue; }
+        if (!dm::boxes_overlap(lo, hi, nl, nh, pad)) { i = escape_from(i, d.besc[i]); continue; }
         const uint32_t cnt = d.bcount[i];
         if (cnt == 0) { ++i; continue; }
         const uint32_t first = d.bfirst[i];
         for (uint32_t k = first; k < first + cnt; ++k) f(d.border[k]);
-        i = d.besc[i];
+        i = escape_from(i, d.besc[i]);
     }
 }
 
@@ -256,14 +262,14 @@ template<class F> __device__ void bvh_query_mixed(const View &d, V lo, V hi, dou
         const float *nl = d.blo32 + 3 * size_t(i), *nh = d.bhi32 + 3 * size_t(i);
         const bool hit = lx <= __fadd_ru(nh[0], p) && nl[0] <= __fadd_ru(hx, p) && ly <= __fadd_ru(nh[1], p) &&
                          nl[1] <= __fadd_ru(hy, p) && lz <= __fadd_ru(nh[2], p) && nl[2] <= __fadd_ru(hz, p);
-        if (!hit) { i = d.besc[i]; continue; }
+        if (!hit) { i = escape_from(i, d.besc[i]); continue; }
         const uint32_t cnt = d.bcount[i];
         if (cnt == 0) { ++i; continue; }
         if (dm::boxes_overlap(lo, hi, load3(d.blo + 3 * size_t(i)), load3(d.bhi + 3 * size_t(i)), pad)) {
             const uint32_t first = d.bfirst[i];
             for (uint32_t k = first; k < first + cnt; ++k) f(d.border[k]);
         }
-        i = d.besc[i];
+        i = escape_from(i, d.besc[i]);
     }
 }
 
@@ -349,13 +355,13 @@ template<class F> __device__ void bvh_positions_packed(const View &d, const Quer
     while (i < d.B) {
         const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
         const uint32_t escape = __float_as_uint(a.w), leaf = __float_as_uint(b.w);
-        if (!maybe_overlap(q, a, b)) { i = escape; continue; }
+        if (!maybe_overlap(q, a, b)) { i = escape_from(i, escape); continue; }
         if (leaf == 0) { ++i; continue; }
         if (leaf_overlap_exact(d, i, a, b, q)) {
             const uint32_t first = leaf >> 4, cnt = leaf & 15u;
             for (uint32_t k = first; k < first + cnt; ++k) f(k);
         }
-        i = escape;
+        i = escape_from(i, escape);
     }
 }
 
@@ -379,11 +385,11 @@ __device__ uint32_t collect_leaves(const View &d, V lo, V hi, double pad, uint32
     while (i < d.B) {
         const float4 a = __ldg(d.bnode + 2 * size_t(i)), b = __ldg(d.bnode + 2 * size_t(i) + 1);
         const uint32_t escape = __float_as_uint(a.w), leaf = __float_as_uint(b.w);
-        if (!maybe_overlap(q, a, b)) { i = escape; continue; }
+        if (!maybe_overlap(q, a, b)) { i = escape_from(i, escape); continue; }
         if (leaf == 0) { ++i; continue; }
         if (n < cap) out[n] = i;
         ++n;
-        i = escape;
+        i = escape_from(i, escape);
     }
     return n;
 }
