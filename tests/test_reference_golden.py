@@ -48,9 +48,9 @@ def test_oracle_one_frame_from_reference_state(oracle_lib, golden, case, frame):
 
 def test_oracle_follows_reference_body_scene_first_frames(oracle_lib, golden):
     """Frames 1-2 of the 265,108-node body scene (no contact yet; the
-    reference repeats them to 3e-9 m) on every 97th node.  Frame 3 is left
-    to the GPU test of the same fixture: on an 8-core host it alone costs
-    two minutes of oracle time."""
+    reference repeats them to 3e-9 m) on every 97th node.  Frame 3 (four
+    minutes of oracle time on an 8-core host) is covered for the GB300
+    library by tests/test_gpu_reference_golden.py."""
     frames = parity.run(oracle_lib, rg.SCENES["body5"](), frames=3)
     report = rg.trajectory_deviation(golden, "body5", frames)
     assert len(report) == 2
